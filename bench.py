@@ -1,0 +1,305 @@
+"""Benchmark: block-parallel IDA* on one GB300 (replicas across GPUs).
+
+Workload (one step = solving the whole batch, every threshold iteration):
+  15-puzzle, 100 uniformly random solvable permutations (seeded Fisher-Yates,
+  parity-fixed), additive 5-5-5 PDB (max of regular and reflected partition),
+  root set ~2048 subproblems per instance, static re-split + in-kernel
+  donation.  Rank r solves its own batch (seed + r): weak scaling, no data
+  collective.
+
+Prints one JSON line (rank 0).  `value` = generated nodes per second with
+the instances already in device memory (sp_solve_batch_device); `e2e` = the
+same through sp_solve_batch with host buffers.  `--impl reference` times the
+reference's serial IDA* restated in C (the oracle) on the host cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "sliding-puzzle_gb300"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "nodes/sec & instances/sec (optimal, exact); learned-LB vs plain LB, 1 GB300"
+UNIT = "nodes/s"
+BYTES_PER_NODE = 64  # 2 table lookups (1 regular + 1 reflected pattern) x 32-byte sector
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in self.lines:
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def workload(rank, n=100):
+    import instances
+    return 4, instances.random_permutations(4, n, seed=0x15B + rank)
+
+
+def cpu_sample(w, states, budget_s, threads):
+    """Oracle on a bounded sample: instances in order, each capped by a node
+    budget, until about budget_s seconds of wall time."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    tabs = oracle.tables(w)
+    # calibrate nodes/s on a short probe, then size the budget
+    t0 = time.perf_counter()
+    probe = oracle.solve(w, states[:threads], oracle.PDB, tabs, threads=threads, node_budget=2_000_000)
+    dt = time.perf_counter() - t0
+    rate = sum(r["nodes_total"] for r in probe) / max(dt, 1e-6)
+    per_inst = max(1_000_000, int(rate * budget_s / max(1, min(len(states), 4 * threads))))
+    sample = states[: min(len(states), 4 * threads)]
+    t0 = time.perf_counter()
+    res = oracle.solve(w, sample, oracle.PDB, tabs, threads=threads, node_budget=per_inst)
+    dt = time.perf_counter() - t0
+    nodes = sum(r["nodes_total"] for r in res)
+    done = sum(1 for r in res if r["status"] == 0)
+    return {"value": nodes / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d instances of the workload, node budget %d each (%d solved), %.1f s" %
+                      (len(sample), per_inst, done, dt),
+            "seconds": dt, "nodes": nodes}
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    w, states = workload(0)
+    threads = os.cpu_count() or 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(w, states, budget_s=args.ref_seconds, threads=threads)
+        if i >= args.warmup:
+            vals.append(r)
+    v = sum(x["nodes"] for x in vals) / sum(x["seconds"] for x in vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * sum(x["seconds"] for x in vals) / len(vals), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded)",
+            "config": {"workload": "15puzzle_random100_pdb555", "instances": len(states),
+                       "solver": "oracle/ida_oracle.c: serial IDA*, one instance per host thread"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": vals[-1]["sample"]},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--instances", type=int, default=100)
+    ap.add_argument("--frontier", type=int, default=2048)
+    ap.add_argument("--lb", default="static")
+    ap.add_argument("--ref-seconds", type=float, default=8.0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    import slide
+
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    w, states = workload(rank, args.instances)
+    n = states.shape[0]
+    solver = slide.Solver(w, "pdb", frontier_target=args.frontier, lb_mode=args.lb)
+    t0 = time.perf_counter()
+    solver.build_pdb()
+    pdb_ms = 1000 * (time.perf_counter() - t0)
+    d_tiles = torch.from_numpy(states.copy()).to("cuda")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    def check(res):
+        lens = []
+        for i in range(n):
+            if res[i].status != 0:
+                raise RuntimeError("instance %d failed with status %d" % (i, res[i].status))
+            lens.append(res[i].len)
+        return lens
+
+    ref_lens = None
+    for _ in range(args.warmup):
+        lens = check(solver.solve_device_raw(d_tiles.data_ptr(), n))
+        ref_lens = ref_lens or lens
+
+    # timed region: device-resident inputs
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    step_ms, kern_ms, nodes, launches, rounds, donated = [], [], 0, 0, 0, 0
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)
+            torch.cuda.synchronize()
+            l0 = slide.kernel_launch_count()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            res = solver.solve_device_raw(d_tiles.data_ptr(), n)
+            e1.record()
+            torch.cuda.synchronize()
+            launches += slide.kernel_launch_count() - l0
+            step_ms.append(e0.elapsed_time(e1))
+            st = solver.stats()
+            kern_ms.append(st["kernel_ms"])
+            rounds += st["rounds"]
+            donated += st["tasks_donated"]
+            if check(res) != ref_lens:
+                raise RuntimeError("lengths changed between steps")
+            nodes += sum(res[i].nodes_total for i in range(n))
+    total_ms = sum(step_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        tn = torch.tensor([nodes], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(tn)
+        total_ms, all_nodes = float(t.item()), float(tn.item())
+    else:
+        all_nodes = float(nodes)
+    value = all_nodes / (total_ms / 1000.0)
+
+    # e2e: host buffers through sp_solve_batch (H2D/D2H inside)
+    e2e_ms, h2d, d2h = [], 0, 0
+    for k in range(args.steps):
+        flush.fill_(k & 0xFF)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        res = solver.solve_raw(states)
+        e1.record()
+        torch.cuda.synchronize()
+        e2e_ms.append(e0.elapsed_time(e1))
+        st = solver.stats()
+        h2d += st["h2d_bytes"] + states.nbytes
+        d2h += st["d2h_bytes"]
+        if [res[i].len for i in range(n)] != ref_lens:
+            raise RuntimeError("e2e lengths differ")
+    e2e_total = sum(e2e_ms)
+    if world > 1:
+        t = torch.tensor([e2e_total], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    e2e_value = all_nodes / (e2e_total / 1000.0)
+
+    peak, peak_kind = load_peaks()
+    kms = sum(kern_ms)
+    achieved = nodes * BYTES_PER_NODE / (kms / 1000.0) / 1e9 if kms > 0 else 0.0
+    traffic = None
+    prof = os.path.join(ROOT, "profiles", "search_round_pdb15_traffic.json")
+    if os.path.exists(prof):
+        traffic = json.load(open(prof)).get("bytes_per_launch")
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_sample(w, states, budget_s=args.cpu_seconds, threads=os.cpu_count() or 1)
+        cpu = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic (seeded)",
+            "config": {"workload": "15puzzle_random100_pdb555", "instances_per_gpu": n,
+                       "heuristic": "additive 5-5-5 PDB, max(regular, reflected)",
+                       "frontier_target": args.frontier, "lb": args.lb + "+donation",
+                       "parallelism": "replicas" if world > 1 else "1 GPU",
+                       "l2": "512 MB buffer written between timed steps",
+                       "pdb_build_ms": round(pdb_ms, 2)},
+            "instances_per_s": world * n / (total_ms / 1000.0),
+            "nodes_per_step": all_nodes / args.steps,
+            "rounds_per_step": rounds / args.steps,
+            "tasks_donated_per_step": donated / args.steps,
+            "kernel_ms_per_step": kms / args.steps,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
+                    "d2h_bytes_per_step": d2h // args.steps, "ms_per_step": e2e_total / args.steps},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "search_round_kernel<4,pdb>", "peak_kind": peak_kind,
+                         "bytes_per_node": BYTES_PER_NODE},
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

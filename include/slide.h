@@ -1,0 +1,166 @@
+/*
+ * slide.h -- C ABI of the GB300 block-parallel IDA* solver (libslide.so).
+ *
+ * The reference has no library API; its de-facto interfaces are
+ *   - per instance: input_table(file) + ida_star(), printing the optimal
+ *     length (src/24puzzle_block_parallel_with_pdb.cu:433, :756, :832) and,
+ *     for the serial solvers, `len node_num` (src/24puzzle_expand.cc:154);
+ *   - per threshold round: dfs_kernel(limit, root_set, dev_flag, loop_set, pdb)
+ *     over a host-built root set (src/24puzzle_block_parallel_with_pdb.cu:524,
+ *     :815), and Horie's idas_kernel(Input*, search_stat*, f_limit, ...)
+ *     (src_horie/idas_smem.cu:282-283);
+ *   - the one host-callable C function
+ *     idas_parallel_main(uchar *input, signed char *plan, int f_limit, ...)
+ *     (src_horie/idas_parallel_host.h:33-34).
+ * Each entry point below names the one it replaces.
+ *
+ * Conventions
+ *   - Tiles: width*width bytes, row-major, 0 is the blank; the goal is
+ *     0 1 2 ... N-1 (blank top-left), as in the reference's instance files.
+ *   - Move codes are the blank's moves: 0 = up, 1 = right, 2 = left,
+ *     3 = down; reverse(d) = 3 - d (src_horie/idas_smem.cu:18-24; the same
+ *     expansion order as src/24puzzle_expand.cc:23-26).
+ *   - Node count: generated children (inside the board, not the reverse of
+ *     the parent's move), summed per threshold iteration; every iteration is
+ *     searched completely, so counts equal the reference's serial
+ *     all-solutions solvers (src/24puzzle_expand.cc:127, :146-164).
+ *   - Every call returns an sp_status (0 = OK, negative = error); nothing
+ *     exits the process or traps the GPU.  Output buffers are caller-owned.
+ *   - A solver owns one CUDA stream and its device memory; it is not
+ *     re-entrant: use one solver per host thread.
+ *   - There is no CPU search path: without a usable GPU, sp_create fails
+ *     with SP_ERR_CUDA.
+ */
+#ifndef SLIDE_H
+#define SLIDE_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SP_MAX_ITERS 96
+#define SP_MAX_MOVES 240
+
+typedef enum {
+  SP_OK = 0,
+  SP_ERR_ARG = -1,
+  SP_ERR_NOT_PERMUTATION = -2,
+  SP_ERR_UNSOLVABLE = -3,
+  SP_ERR_LIMIT = -4,          /* no solution within SP_MAX_ITERS thresholds */
+  SP_ERR_CUDA = -5,           /* a CUDA call failed (message: sp_last_error) */
+  SP_ERR_NO_PDB = -6,         /* PDB heuristic selected but tables not built */
+  SP_ERR_STACK_OVERFLOW = -7, /* a subtree deeper than the per-lane stack */
+  SP_ERR_TIMEOUT = -8,        /* a device wait made no progress in time */
+  SP_ERR_CAPACITY = -9,       /* a host-side table would exceed its limit */
+  SP_ERR_PATH = -10           /* a solution path longer than SP_MAX_MOVES */
+} sp_status;
+
+typedef enum { SP_HEUR_MANHATTAN = 0, SP_HEUR_PDB = 1 } sp_heuristic_kind;
+
+typedef enum {
+  SP_LB_STEAL = 0,         /* dynamic donation through the device task pool */
+  SP_LB_STATIC_STEAL = 1,  /* + reference-style static re-split from the
+                              previous round's loads
+                              (src/24puzzle_block_parallel_with_pdb.cu:839-897) */
+  SP_LB_NONE = 2           /* root set only: no re-split, no donation */
+} sp_lb_mode;
+
+typedef struct {
+  int32_t frontier_target;   /* subproblems per instance (reference BLOCK_NUM 2048) */
+  int32_t threads_per_block; /* 128 or 256 */
+  int32_t blocks_per_sm;     /* 0 = occupancy maximum */
+  int32_t lb_mode;           /* sp_lb_mode */
+  int32_t donate_min_slack;  /* donate a branch only if limit - depth >= this */
+  int32_t steps_per_poll;    /* DFS steps between task-pool polls */
+  int32_t timeout_ms;        /* device no-progress limit for pool waits */
+  int32_t static_split_cap;  /* max pieces one root is split into (static LB) */
+} sp_config;
+
+/* One instance's answer: "state in, optimal move sequence and per-iteration
+ * node counts out" (the reference's ida_star() prints only `len [nodes]`). */
+typedef struct {
+  int32_t status;
+  int32_t len;               /* optimal solution length, -1 if none */
+  int32_t n_iter;            /* completed threshold iterations */
+  int32_t n_moves;           /* == len when solved */
+  uint64_t nodes_total;
+  int32_t f_limit[SP_MAX_ITERS];
+  uint64_t nodes[SP_MAX_ITERS];
+  uint8_t moves[SP_MAX_MOVES];
+  double seconds;            /* wall time of the batch this instance was in */
+} sp_result;
+
+typedef struct {
+  double frontier_ms;        /* host root-set construction */
+  double kernel_ms;          /* device time of the round kernels (events) */
+  double wall_ms;            /* whole call */
+  int32_t rounds;
+  int32_t kernel_launches;   /* this library's kernels launched by the call */
+  uint64_t tasks_initial;    /* root subproblems started, summed over rounds */
+  uint64_t tasks_donated;    /* tasks created by in-kernel donation */
+  uint64_t nodes;            /* generated nodes, all instances, all rounds */
+  uint64_t h2d_bytes, d2h_bytes;
+} sp_stats;
+
+typedef struct sp_solver sp_solver;
+
+void sp_config_default(sp_config *cfg);
+
+/* Create a solver for width 4 (15-puzzle) or 5 (24-puzzle).  cfg may be
+ * NULL.  Replaces the reference's per-program globals and main() set-up
+ * (src/24puzzle_block_parallel_with_pdb.cu:925-944). */
+int sp_create(int width, int heuristic, const sp_config *cfg, sp_solver **out);
+void sp_destroy(sp_solver *s);
+int sp_set_config(sp_solver *s, const sp_config *cfg);
+
+/* Build the additive pattern databases on the GPU by breadth-first search
+ * (width 4: this project's 5-5-5 partition; width 5: the reference's 6-6-6-6
+ * tables {1,2,5,6,7,12} and {3,4,8,9,13,14}).  Replaces reading the absent
+ * pat24.*.tab files (src/24puzzle_block_parallel_with_pdb.cu:164-230). */
+int sp_pdb_build(sp_solver *s);
+uint64_t sp_pdb_table_size(int width);   /* n!/(n-k)! bytes per table */
+int sp_pdb_num_tables(int width);
+/* Tables in compact rank order: the byte order of the reference's table
+ * files, read by src/24puzzle_block_parallel_with_pdb.cu:177-230. */
+int sp_pdb_export(sp_solver *s, int table, uint8_t *dst, uint64_t size);
+int sp_pdb_import(sp_solver *s, int table, const uint8_t *src, uint64_t size);
+
+/* Heuristic value of n states (tiles n*width*width) into h[n]. */
+int sp_heuristic(sp_solver *s, const uint8_t *tiles, int n, int32_t *h);
+
+/* Solve n instances, results[n].  Replaces input_table() + ida_star()
+ * (src/24puzzle_block_parallel_with_pdb.cu:433-452, :756-922), batched: all
+ * instances share each threshold round's kernel launch. */
+int sp_solve_batch(sp_solver *s, const uint8_t *tiles, int n, sp_result *results);
+
+/* The same with the instances already in device memory (d_tiles is a device
+ * pointer to n*width*width bytes). */
+int sp_solve_batch_device(sp_solver *s, const void *d_tiles, int n, sp_result *results);
+
+/* One threshold round over a caller-built root set: the drop-in for
+ * dfs_kernel<<<root_node_size, 32>>>(limit, root_set, dev_flag, loop_set, pdb)
+ * (src/24puzzle_block_parallel_with_pdb.cu:524, :815-822).
+ *   roots      n*width*width tiles        (root_set[i].puzzle)
+ *   depth[i]   g of root i                 (root_set[i].depth)
+ *   pre[i]     move that produced root i, -1 if none (root_set[i].pre)
+ *   limit      f-limit of the round
+ *   nodes[i]   out: generated children in root i's subtree, root included
+ *              if depth+h <= limit (the reference's loop_set counts rounds
+ *              of its block loop; this counts nodes)
+ *   found      out: shortest goal depth seen, -1 if none (dev_flag) */
+int sp_dfs_round(sp_solver *s, const uint8_t *roots, const int32_t *depth,
+                 const int32_t *pre, int n, int limit, uint64_t *nodes,
+                 int32_t *found);
+
+int sp_last_stats(const sp_solver *s, sp_stats *out);
+const char *sp_status_string(int status);
+const char *sp_last_error(const sp_solver *s);
+/* Device kernels this library launched since load (evidence counter). */
+uint64_t sp_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,533 @@
+// Threshold-round search kernel of libslide.
+//
+// One launch searches one IDA* threshold for every unsolved instance of a
+// batch.  It replaces the reference's per-round dfs_kernel
+// (src/24puzzle_block_parallel_with_pdb.cu:520-648: one 32-thread block per
+// root, 8 nodes x 4 moves per round, three __syncthreads per round, a
+// 326-entry shared Node stack) with:
+//
+//  * one lane = one depth-first search over a task (a root-set node, possibly
+//    narrowed to some of its first moves); no block barriers in the loop;
+//  * the lane's path kept as 2-bit moves in shared memory (a [word][lane]
+//    layout, so lanes never conflict on banks) and undone move by move;
+//  * 15-puzzle boards packed 4 bits per cell in one 64-bit register, 24-puzzle
+//    boards as bytes in shared memory;
+//  * Manhattan distance updated from a per-(move, cell, tile) delta table in
+//    shared memory (src/15puzzle_block_parallel.cu:271-272 updates it with two
+//    constant-memory lookups);
+//  * PDB indices kept per pattern as mixed-radix integers and updated by one
+//    add per move, so a move costs one regular and one reflected table lookup
+//    instead of the reference's eight (src/24puzzle_block_parallel_with_pdb.cu
+//    :426-429); the idea of updating only the moved tile's pattern is Horie's
+//    (src_horie/idas_pdb.cu:221-254);
+//  * load balance by a device task pool: lanes claim slots warp-aggregated
+//    (ballot + one atomicAdd per warp); claims may run ahead of the pool's
+//    tail, and while any lane waits, busy lanes donate the untried moves of
+//    their shallowest open level as a new task (the reference's closest
+//    counterpart is Horie's intra-warp sharing, src_horie/idas_dynamic.cu
+//    :200-247; the reference's own balance is the host re-split of
+//    :839-897, done by the host round loop here).
+//
+// Every wait is bounded: a warp whose lanes all wait and see no change of the
+// pool for timeout_ns sets SP_ERR_TIMEOUT and every warp returns.  Nothing
+// traps.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/slide.h"
+#include "sp_defs.h"
+#include "sp_kernels.h"
+
+namespace sp {
+
+namespace {
+
+__device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p) {
+  return *(const volatile uint32_t *)p;
+}
+__device__ __forceinline__ int32_t ld_volatile(const int32_t *p) {
+  return *(const volatile int32_t *)p;
+}
+__device__ __forceinline__ unsigned long long globaltimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Pattern-index field helpers.  Width 4: three 20-bit indices in one u64 per
+// partition.  Width 5: four 28-bit indices, two per u64.
+template <int W>
+struct Idx;
+
+template <>
+struct Idx<4> {
+  uint64_t a;
+  __device__ __forceinline__ void clear() { a = 0; }
+  __device__ __forceinline__ uint32_t get(int p) const { return (uint32_t)(a >> (20 * p)) & 0xFFFFFu; }
+  __device__ __forceinline__ void add(int p, int32_t d) { a += (uint64_t)((int64_t)d << (20 * p)); }
+};
+
+template <>
+struct Idx<5> {
+  uint64_t a, b;
+  __device__ __forceinline__ void clear() { a = b = 0; }
+  __device__ __forceinline__ uint32_t get(int p) const {
+    uint64_t w = (p >> 1) ? b : a;
+    return (uint32_t)(w >> (28 * (p & 1))) & 0xFFFFFFFu;
+  }
+  __device__ __forceinline__ void add(int p, int32_t d) {
+    uint64_t v = (uint64_t)((int64_t)d << (28 * (p & 1)));
+    if (p >> 1) b += v; else a += v;
+  }
+};
+
+__device__ __forceinline__ uint32_t byte_sum(uint32_t v) { return __dp4a(v, 0x01010101u, 0u); }
+__device__ __forceinline__ uint32_t set_byte(uint32_t v, int p, uint32_t x) {
+  return (v & ~(0xFFu << (8 * p))) | (x << (8 * p));
+}
+
+}  // namespace
+
+template <int W, bool PDB, int BLOCK, int WORDS>
+__global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
+  constexpr int N = W * W;
+  constexpr int BSTRIDE = 28;  // bytes per lane board (7 words: conflict-free same-cell access)
+  constexpr int MAXLEV = WORDS * 16;
+  constexpr unsigned FULL = 0xffffffffu;
+  __shared__ uint32_t s_code[PDB ? 2 * N * N : 1];
+  __shared__ uint8_t s_pat[PDB ? 2 * N : 1];
+  __shared__ int8_t s_mdd[PDB ? 1 : 4 * N * N];
+  __shared__ uint32_t s_stack[WORDS][BLOCK];
+  __shared__ __align__(16) uint8_t s_board[W == 5 ? BLOCK * BSTRIDE : 4];
+
+  const HeurTables *ht = P.ht;
+  if (PDB) {
+    for (int i = threadIdx.x; i < N * N; i += BLOCK) {
+      s_code[i] = ht->code[0][i];
+      s_code[N * N + i] = ht->code[1][i];
+    }
+    for (int i = threadIdx.x; i < N; i += BLOCK) {
+      s_pat[i] = ht->pat[0][i];
+      s_pat[N + i] = ht->pat[1][i];
+    }
+  } else {
+    for (int i = threadIdx.x; i < 4 * N * N; i += BLOCK) s_mdd[i] = ht->mdd[i];
+  }
+  __syncthreads();
+
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  uint8_t *myboard = s_board + (W == 5 ? tid * BSTRIDE : 0);
+  PoolCtl *ctl = P.ctl;
+
+  // ---- lane state -------------------------------------------------------
+  int state = 0;  // 0 idle, 1 holds a claimed slot, 2 searching
+  uint32_t slot = 0;
+  uint64_t b64 = 0;  // width-4 board
+  int blank = 0, g = 0, h = 0, k = 0, it = 0, pre = -1, limit = 0;
+  int rblank = 0, rpre = -1, groot = 0, plen = 0;
+  uint32_t mask0 = 0, top = 0, sub = 0;
+  uint64_t cut = 0;
+  unsigned long long cnt = 0;
+  Idx<W> ir, iff;
+  uint32_t hvr = 0, hvf = 0;
+  ir.clear();
+  iff.clear();
+
+  auto tile_at = [&](int c) -> int {
+    if (W == 4) return (int)((b64 >> (4 * c)) & 15u);
+    return myboard[c];
+  };
+  // slide tile t from cell `from` into the blank at cell `to`
+  auto slide = [&](int t, int from, int to) {
+    if (W == 4) {
+      b64 ^= ((uint64_t)t << (4 * from)) ^ ((uint64_t)t << (4 * to));
+    } else {
+      myboard[to] = (uint8_t)t;
+      myboard[from] = 0;
+    }
+  };
+  auto lookup = [&](int p, uint32_t idx) -> uint32_t {
+    size_t off = (W == 4) ? ((size_t)p << 20) : (p ? ((size_t)1 << 28) : 0);
+    return __ldg(P.pdb + off + idx);
+  };
+  auto stack_dir = [&](int i) -> int {
+    uint32_t w = ((i >> 4) < (k >> 4)) ? s_stack[i >> 4][tid] : top;
+    return (int)((w >> (2 * (i & 15))) & 3u);
+  };
+  auto task_dir = [&](int i) -> int {
+    uint32_t w = __ldcg(&P.tasks[slot].path[i >> 4]);
+    return (int)((w >> (2 * (i & 15))) & 3u);
+  };
+  // moves 0..len-1 of the lane's path below its SubRoot: task prefix then stack
+  auto path_word = [&](int wi, int len) -> uint32_t {
+    uint32_t out = 0;
+    for (int b = 0; b < 16; ++b) {
+      int j = wi * 16 + b;
+      if (j >= len) break;
+      int d = j < plen ? task_dir(j) : stack_dir(j - plen);
+      out |= (uint32_t)d << (2 * b);
+    }
+    return out;
+  };
+  auto full_h = [&]() -> int {
+    if (PDB) {
+      ir.clear();
+      iff.clear();
+      for (int c = 0; c < N; ++c) {
+        int t = tile_at(c);
+        if (!t) continue;
+        ir.add(s_pat[t], (int32_t)s_code[t * N + c]);
+        iff.add(s_pat[N + t], (int32_t)s_code[N * N + t * N + c]);
+      }
+      hvr = hvf = 0;
+      constexpr int NP = (W == 5) ? 4 : 3;
+      for (int p = 0; p < NP; ++p) {
+        hvr = set_byte(hvr, p, lookup(W == 5 ? (p != 0) : p, ir.get(p)));
+        hvf = set_byte(hvf, p, lookup(W == 5 ? (p != 0) : p, iff.get(p)));
+      }
+      return (int)max(byte_sum(hvr), byte_sum(hvf));
+    } else {
+      int s = 0;
+      for (int c = 0; c < N; ++c) {
+        int t = tile_at(c);
+        if (!t) continue;
+        int dr = c / W - t / W, dc = c % W - t % W;
+        s += abs(dr) + abs(dc);
+      }
+      return s;
+    }
+  };
+  auto set_error = [&](int code, uint32_t info) {
+    if (atomicCAS(&ctl->error, 0, code) == 0) ctl->err_info[0] = info;
+  };
+  auto finish_task = [&]() {
+    if (cnt) atomicAdd(&P.sub_nodes[sub], cnt);
+    __threadfence();
+    atomicSub(&ctl->outstanding, 1u);
+    state = 0;
+  };
+  auto start_task = [&]() -> bool {
+    const Task *T = &P.tasks[slot];
+    sub = __ldcg(&T->sub);
+    uint32_t hdr = __ldcg((const uint32_t *)T + 1);
+    plen = (int)(hdr & 0xFFFFu);
+    mask0 = (hdr >> 16) & 0xFu;
+    const SubRoot *R = &P.subs[sub];
+    const uint8_t *rb = R->board;
+    if (W == 4) {
+      uint4 v = *(const uint4 *)rb;
+      const uint8_t *bb = (const uint8_t *)&v;
+      b64 = 0;
+      for (int c = 0; c < 16; ++c) b64 |= (uint64_t)(bb[c] & 15u) << (4 * c);
+    } else {
+      for (int c = 0; c < N; ++c) myboard[c] = rb[c];
+    }
+    uint4 tailv = *(const uint4 *)(rb + 16);
+    const uint8_t *tb = (const uint8_t *)&tailv;
+    blank = tb[25 - 16];
+    g = tb[26 - 16];
+    pre = tb[27 - 16] == kNoPre ? -1 : (int)tb[27 - 16];
+    uint32_t inst = *(const uint32_t *)(tb + 12);
+    limit = P.inst_limit[inst];
+    for (int i = 0; i < plen; ++i) {
+      int d = task_dir(i);
+      int src = blank + move_delta(W, d);
+      slide(tile_at(src), src, blank);
+      blank = src;
+      pre = d;
+      ++g;
+    }
+    h = full_h();
+    rblank = blank;
+    rpre = pre;
+    groot = g;
+    k = 0;
+    it = 0;
+    top = 0;
+    cut = 0;
+    cnt = 0;
+    return g + h <= limit;
+  };
+  auto record_goal = [&]() {
+    Solution *S = &P.sol[P.subs[sub].inst];
+    if (atomicCAS(&S->flag, 0u, 1u) == 0u) {
+      int len = plen + k;
+      S->sub = sub;
+      S->len = (uint32_t)len;
+      for (int wi = 0; wi < kPathWords; ++wi) S->path[wi] = path_word(wi, len);
+      __threadfence();
+    }
+  };
+
+  // One edge of the depth-first search: generate the next child of the
+  // current node, or backtrack.  Returns true when the task is exhausted.
+  auto step = [&]() -> bool {
+    uint32_t cand = legal_moves(W, blank) & (0xFu << it);
+    if (pre >= 0) cand &= ~(1u << (3 - pre));
+    if (k == 0) cand &= mask0;
+    if (cand) {
+      const int d = __ffs(cand) - 1;
+      const int src = blank + move_delta(W, d);
+      const int t = tile_at(src);
+      ++cnt;
+      int nh;
+      uint32_t nhvr = hvr, nhvf = hvf;
+      Idx<W> nir = ir, nif = iff;
+      if (PDB) {
+        const int pr = s_pat[t], pf = s_pat[N + t];
+        nir.add(pr, (int32_t)(s_code[t * N + blank] - s_code[t * N + src]));
+        nif.add(pf, (int32_t)(s_code[N * N + t * N + blank] - s_code[N * N + t * N + src]));
+        nhvr = set_byte(hvr, pr, lookup(W == 5 ? (pr != 0) : pr, nir.get(pr)));
+        nhvf = set_byte(hvf, pf, lookup(W == 5 ? (pf != 0) : pf, nif.get(pf)));
+        nh = (int)max(byte_sum(nhvr), byte_sum(nhvf));
+      } else {
+        nh = h + s_mdd[(d * N + src) * N + t];
+      }
+      if (g + 1 + nh <= limit) {
+        if (k + 1 >= MAXLEV || plen + k + 1 > kMaxPath) {
+          set_error(SP_ERR_STACK_OVERFLOW, (uint32_t)(plen + k));
+          return true;
+        }
+        slide(t, src, blank);
+        blank = src;
+        ++g;
+        h = nh;
+        if (PDB) { ir = nir; iff = nif; hvr = nhvr; hvf = nhvf; }
+        const int sh = 2 * (k & 15);
+        top = (top & ~(3u << sh)) | ((uint32_t)d << sh);
+        if ((k & 15) == 15) s_stack[k >> 4][tid] = top;
+        ++k;
+        if (k < 64) cut &= ~(1ull << k);
+        pre = d;
+        it = 0;
+        if (nh == 0) record_goal();
+      } else {
+        it = d + 1;
+      }
+      return false;
+    }
+    if (k == 0) return true;
+    --k;
+    if ((k & 15) == 15) top = s_stack[k >> 4][tid];
+    const int d = (int)((top >> (2 * (k & 15))) & 3u);
+    const int back = blank - move_delta(W, d);
+    const int t = tile_at(back);
+    // the tile returns from `back` to the blank's cell
+    if (PDB) {
+      const int pr = s_pat[t], pf = s_pat[N + t];
+      ir.add(pr, (int32_t)(s_code[t * N + blank] - s_code[t * N + back]));
+      iff.add(pf, (int32_t)(s_code[N * N + t * N + blank] - s_code[N * N + t * N + back]));
+      hvr = set_byte(hvr, pr, lookup(W == 5 ? (pr != 0) : pr, ir.get(pr)));
+      hvf = set_byte(hvf, pf, lookup(W == 5 ? (pf != 0) : pf, iff.get(pf)));
+      h = (int)max(byte_sum(hvr), byte_sum(hvf));
+    } else {
+      h -= s_mdd[(d * N + blank) * N + t];
+    }
+    slide(t, back, blank);
+    blank = back;
+    --g;
+    it = d + 1;
+    if (k < 64 && ((cut >> k) & 1ull)) it = 4;
+    if (k == 0) pre = rpre;
+    else if (k & 15) pre = (int)((top >> (2 * ((k - 1) & 15))) & 3u);
+    else pre = (int)((s_stack[(k - 1) >> 4][tid] >> 30) & 3u);
+    return false;
+  };
+
+  // Give the untried moves of the shallowest open level (slack >= min_slack)
+  // to a waiting lane.  Returns the level donated, or -1.
+  auto find_donation = [&](uint32_t &mask_out) -> int {
+    int bl = rblank, pr = rpre;
+    const int lim = min(k, 63);
+    for (int j = 0; j <= lim; ++j) {
+      if (limit - (groot + j) < P.min_slack) return -1;
+      uint32_t un;
+      if (j == k) {
+        un = legal_moves(W, bl) & (0xFu << it);
+      } else {
+        const int dj = stack_dir(j);
+        un = legal_moves(W, bl) & (0xFu << (dj + 1)) & 0xFu;
+        bl += move_delta(W, dj);
+        if (pr >= 0) un &= ~(1u << (3 - pr));
+        if (j == 0) un &= mask0;
+        pr = dj;
+        if (!((cut >> j) & 1ull) && un) { mask_out = un; return j; }
+        continue;
+      }
+      if (pr >= 0) un &= ~(1u << (3 - pr));
+      if (j == 0) un &= mask0;
+      if (!((cut >> j) & 1ull) && un) { mask_out = un; return j; }
+    }
+    return -1;
+  };
+
+  unsigned long long last_change = 0;
+  uint32_t last_out = 0xFFFFFFFFu, last_tail = 0xFFFFFFFFu;
+
+  for (;;) {
+    // 1. idle lanes claim pool slots, one atomic per warp
+    const unsigned need = __ballot_sync(FULL, state == 0);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(&ctl->head, (uint32_t)__popc(need));
+      base = __shfl_sync(FULL, base, leader);
+      if (state == 0) {
+        slot = base + (uint32_t)__popc(need & ((1u << lane) - 1u));
+        state = 1;
+      }
+    }
+    // 2. a claimed slot becomes a task once its producer published it
+    if (state == 1 && slot < P.cap && ld_volatile(&P.ready[slot]) == P.stamp) {
+      __threadfence();
+      if (start_task()) state = 2;
+      else finish_task();
+    }
+    // 3. nobody in the warp is searching: finished, failed or waiting
+    const unsigned act = __ballot_sync(FULL, state == 2);
+    if (!act) {
+      uint32_t out = 0, tl = 0;
+      int32_t err = 0;
+      if (lane == 0) {
+        out = ld_volatile(&ctl->outstanding);
+        tl = ld_volatile(&ctl->tail);
+        err = ld_volatile(&ctl->error);
+        const unsigned long long now = globaltimer();
+        if (out != last_out || tl != last_tail || last_change == 0) {
+          last_out = out;
+          last_tail = tl;
+          last_change = now;
+        } else if (now - last_change > P.timeout_ns) {
+          set_error(SP_ERR_TIMEOUT, out);
+          err = SP_ERR_TIMEOUT;
+        }
+      }
+      out = __shfl_sync(FULL, out, 0);
+      err = __shfl_sync(FULL, err, 0);
+      if (out == 0 || err != 0) break;
+      __nanosleep(500);
+      continue;
+    }
+    // 4. search
+    if (state == 2) {
+      for (int s = 0; s < P.steps; ++s) {
+        if (step()) {
+          finish_task();
+          break;
+        }
+      }
+    }
+    // 5. pool status: errors and hunger
+    uint32_t hd = 0, tl = 0;
+    int32_t err = 0;
+    if (lane == 0) {
+      hd = ld_volatile(&ctl->head);
+      tl = ld_volatile(&ctl->tail);
+      err = ld_volatile(&ctl->error);
+    }
+    hd = __shfl_sync(FULL, hd, 0);
+    tl = __shfl_sync(FULL, tl, 0);
+    err = __shfl_sync(FULL, err, 0);
+    if (err) break;
+    if (P.donate && hd > tl && tl < P.cap) {
+      uint32_t dmask = 0;
+      int lev = (state == 2) ? find_donation(dmask) : -1;
+      // one donor per warp per poll: the lane with the shallowest level
+      const unsigned key = lev >= 0 ? ((unsigned)lev << 5) | (unsigned)lane : 0xFFFFFFFFu;
+      const unsigned best = __reduce_min_sync(FULL, key);
+      if (best != 0xFFFFFFFFu && (int)(best & 31u) == lane) {
+        uint32_t t = ld_volatile(&ctl->tail), hh = ld_volatile(&ctl->head);
+        bool ok = false;
+        while (t < hh && t < P.cap) {
+          const uint32_t old = atomicCAS(&ctl->tail, t, t + 1);
+          if (old == t) { ok = true; break; }
+          t = old;
+          hh = ld_volatile(&ctl->head);
+        }
+        if (ok && plen + lev <= kMaxPath) {
+          atomicAdd(&ctl->outstanding, 1u);
+          Task *D = &P.tasks[t];
+          const int nlen = plen + lev;
+          D->sub = sub;
+          D->plen = (uint16_t)nlen;
+          D->mask = (uint8_t)dmask;
+          D->flags = 1;
+          for (int wi = 0; wi < kPathWords; ++wi) D->path[wi] = path_word(wi, nlen);
+          __threadfence();
+          atomicExch(&P.ready[t], P.stamp);
+          atomicAdd(&ctl->donated, 1ull);
+          if (lev == k) it = 4;
+          else cut |= 1ull << lev;
+        } else if (ok) {
+          // cannot encode the prefix: publish an empty task so the slot's claimant moves on
+          atomicAdd(&ctl->outstanding, 1u);
+          Task *D = &P.tasks[t];
+          D->sub = sub;
+          D->plen = 0;
+          D->mask = 0;
+          D->flags = 2;
+          __threadfence();
+          atomicExch(&P.ready[t], P.stamp);
+        }
+      }
+    }
+  }
+}
+
+// Fill the first n pool slots with the round's root tasks and publish them.
+__global__ void pool_init_kernel(Task *tasks, const Task *init, uint32_t *ready, uint32_t n,
+                                 uint32_t stamp, PoolCtl *ctl) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    tasks[i] = init[i];
+    ready[i] = stamp;
+  }
+  if (i == 0) {
+    ctl->head = 0;
+    ctl->tail = n;
+    ctl->outstanding = n;
+    ctl->error = 0;
+    ctl->donated = 0;
+    ctl->progress_ns = 0;
+  }
+}
+
+// Host launchers (template kernels stay in this translation unit).
+cudaError_t launch_search_round(int w, bool pdb, int block, int blocks_per_sm, int num_sms,
+                                const RoundParams &P, cudaStream_t st, int *grid_out) {
+  void (*kern)(RoundParams) = nullptr;
+#define SP_PICK(W, PD, B, WD) \
+  if (w == W && pdb == PD && block == B) kern = search_round_kernel<W, PD, B, WD>;
+  SP_PICK(4, false, 256, 6)
+  SP_PICK(4, true, 256, 6)
+  SP_PICK(5, false, 256, 10)
+  SP_PICK(5, true, 256, 10)
+  SP_PICK(4, false, 128, 6)
+  SP_PICK(4, true, 128, 6)
+  SP_PICK(5, false, 128, 10)
+  SP_PICK(5, true, 128, 10)
+#undef SP_PICK
+  if (!kern) return cudaErrorInvalidValue;
+  int per_sm = blocks_per_sm;
+  if (per_sm <= 0) {
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, 0);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+  }
+  const int grid = num_sms * per_sm;
+  if (grid_out) *grid_out = grid;
+  kern<<<grid, block, 0, st>>>(P);
+  note_launch();
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pool_init(Task *tasks, const Task *init, uint32_t *ready, uint32_t n,
+                             uint32_t stamp, PoolCtl *ctl, cudaStream_t st) {
+  const uint32_t blocks = n ? (n + 255) / 256 : 1;
+  pool_init_kernel<<<blocks, 256, 0, st>>>(tasks, init, ready, n, stamp, ctl);
+  note_launch();
+  return cudaGetLastError();
+}
+
+}  // namespace sp

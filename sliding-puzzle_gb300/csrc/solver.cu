@@ -1,0 +1,909 @@
+// Host side of libslide: the C ABI (include/slide.h), the root-set
+// ("frontier") construction, the IDA* threshold-round loop and static load
+// balancing.  Device work is in search.cu and pdb_build.cu.
+//
+// Reference counterparts:
+//   create_root_set       src/24puzzle_block_parallel_with_pdb.cu:454-490
+//   ida_star round loop   src/24puzzle_block_parallel_with_pdb.cu:756-922
+//   divide_root_set       src/24puzzle_block_parallel_with_pdb.cu:652-747
+//
+// Differences that keep node counts exact (the reference's GPU solvers
+// report lengths only):
+//   * the root set is a tree expansion to a uniform depth with no duplicate
+//     detection (Horie's A* distribution merges transpositions,
+//     src_horie/idas_smem.cu:1083-1113, which changes counts);
+//   * a goal met while building the root set does not end the search early
+//     (src/24puzzle_block_parallel_with_pdb.cu:482-485 returns there);
+//   * each round adds the children generated by root-set interior nodes
+//     whose path stays within the limit (prefix maximum of g+h: the PDB
+//     heuristic is not consistent, so f can drop along a path), and a root
+//     becomes a device task only if the same holds for it;
+//   * the static re-split of heavy roots (ceil(load/avg) pieces, as at
+//     :839-897) refines the root-set tree, so the pieces' ancestors are
+//     counted like any other interior node.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cstdio>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/slide.h"
+#include "sp_defs.h"
+#include "sp_kernels.h"
+
+namespace sp {
+
+static std::atomic<uint64_t> g_launches{0};
+void note_launch(int n) { g_launches.fetch_add((uint64_t)n); }
+
+namespace {
+
+struct TreeNode {
+  uint8_t board[kMaxN];
+  uint8_t blank, g, pre, move;  // move: from parent (kNoPre for the root)
+  int32_t parent;
+  int32_t h;
+  int32_t maxf;                 // max of g+h over the path root..this node
+  uint8_t nchild;               // legal non-reverse children
+  uint8_t leaf;                 // 1: root-set member (device task when active)
+  uint8_t expanded;             // children present in the tree
+  uint8_t pad;
+  int32_t sub;                  // index into the batch's SubRoot array, -1 if none
+};
+
+struct Instance {
+  int status = SP_OK;
+  int h0 = 0;
+  int iter = 0;
+  bool done = false;
+  std::vector<TreeNode> tree;
+  std::vector<int32_t> leaves;      // tree indices of root-set members
+  std::vector<uint64_t> last_load;  // per leaf, previous round
+  sp_result *out = nullptr;
+};
+
+double ms_since(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+int check_instance(int w, const uint8_t *t) {
+  const int n = w * w;
+  uint32_t seen = 0;
+  for (int i = 0; i < n; ++i) {
+    if (t[i] >= n || ((seen >> t[i]) & 1u)) return SP_ERR_NOT_PERMUTATION;
+    seen |= 1u << t[i];
+  }
+  int inv = 0, brow = 0;
+  for (int i = 0; i < n; ++i) {
+    if (!t[i]) { brow = i / w; continue; }
+    for (int j = i + 1; j < n; ++j)
+      if (t[j] && t[j] < t[i]) ++inv;
+  }
+  // goal blank at cell 0: odd widths keep inversion parity; even widths keep
+  // inversions + blank row
+  const int par = (w & 1) ? (inv & 1) : ((inv + brow) & 1);
+  return par ? SP_ERR_UNSOLVABLE : SP_OK;
+}
+
+}  // namespace
+}  // namespace sp
+
+using namespace sp;
+
+struct sp_solver {
+  int w = 4, n = 16, heur = SP_HEUR_MANHATTAN;
+  sp_config cfg{};
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int num_sms = 0;
+  HeurTables h_ht{};
+  HeurTables *d_ht = nullptr;
+  uint8_t *d_pdb = nullptr;
+  bool pdb_ready = false;
+  uint32_t import_mask = 0;
+  double pdb_build_ms = 0;
+  int last_grid = 0;
+  // device task pool
+  Task *d_tasks = nullptr;
+  uint32_t *d_ready = nullptr;
+  uint32_t cap = 0;
+  PoolCtl *d_ctl = nullptr;
+  uint32_t stamp = 0;
+  // per-batch buffers
+  SubRoot *d_subs = nullptr;
+  size_t subs_cap = 0;
+  Task *d_init = nullptr;
+  size_t init_cap = 0;
+  unsigned long long *d_sub_nodes = nullptr;
+  int32_t *d_limit = nullptr;
+  Solution *d_sol = nullptr;
+  size_t inst_cap = 0;
+  uint8_t *d_boards = nullptr;
+  int32_t *d_h = nullptr;
+  size_t boards_cap = 0;
+  size_t h_cap = 0;
+  std::string err;
+  sp_stats stats{};
+};
+
+namespace {
+
+int fail_cuda(sp_solver *s, cudaError_t e, const char *what) {
+  s->err = std::string(what) + ": " + cudaGetErrorString(e);
+  return SP_ERR_CUDA;
+}
+
+#define SP_CUDA(s, call)                                      \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return fail_cuda((s), e_, #call); \
+  } while (0)
+
+template <typename T>
+int ensure(sp_solver *s, T **p, size_t *cap, size_t need) {
+  if (*cap >= need && *p) return SP_OK;
+  size_t ncap = std::max(need, *cap * 2);
+  if (ncap < 64) ncap = 64;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  SP_CUDA(s, cudaMalloc((void **)p, ncap * sizeof(T)));
+  *cap = ncap;
+  return SP_OK;
+}
+
+void build_heur_tables(int w, HeurTables *ht) {
+  memset(ht, 0, sizeof(*ht));
+  const int n = w * w;
+  for (int d = 0; d < 4; ++d)
+    for (int c = 0; c < n; ++c)
+      for (int t = 0; t < n; ++t) {
+        // the blank moved by d onto cell c; the tile t at c slides back to b
+        const int b = c - move_delta(w, d);
+        int v = 0;
+        if (t && b >= 0 && b < n) {
+          const int mb = abs(b / w - t / w) + abs(b % w - t % w);
+          const int mc = abs(c / w - t / w) + abs(c % w - t % w);
+          v = mb - mc;
+        }
+        ht->mdd[(d * n + c) * n + t] = (int8_t)v;
+      }
+  PatternSet ps = pattern_set(w);
+  for (int part = 0; part < 2; ++part) {
+    for (int t = 0; t < n; ++t) ht->pat[part][t] = 0xFF;
+    for (int p = 0; p < ps.n_pat; ++p) {
+      const int tab = ps.pat_table[part][p], sym = ps.pat_sym[part][p];
+      for (int j = 0; j < ps.k; ++j) {
+        // tile whose goal cell maps onto the table's j-th goal cell
+        int tile = -1;
+        for (int c = 0; c < n; ++c)
+          if (sym_cell(w, sym, c) == ps.table_tiles[tab][j]) tile = c;
+        uint32_t mul = 1;
+        for (int q = j + 1; q < ps.k; ++q) mul *= (uint32_t)ps.radix;
+        ht->pat[part][tile] = (uint8_t)p;
+        for (int c = 0; c < n; ++c) ht->code[part][tile * n + c] = (uint32_t)sym_cell(w, sym, c) * mul;
+      }
+    }
+  }
+}
+
+void make_root(int w, const uint8_t *tiles, TreeNode *r) {
+  memset(r, 0, sizeof(*r));
+  const int n = w * w;
+  for (int i = 0; i < n; ++i) {
+    r->board[i] = tiles[i];
+    if (!tiles[i]) r->blank = (uint8_t)i;
+  }
+  r->g = 0;
+  r->pre = kNoPre;
+  r->move = kNoPre;
+  r->parent = -1;
+  r->sub = -1;
+}
+
+// Append the children of tree[idx]; returns how many.
+int expand_node(int w, std::vector<TreeNode> &tree, int idx) {
+  TreeNode p = tree[idx];
+  uint32_t mv = legal_moves(w, p.blank);
+  if (p.pre != kNoPre) mv &= ~(1u << (3 - p.pre));
+  int cnt = 0;
+  for (int d = 0; d < 4; ++d) {
+    if (!((mv >> d) & 1u)) continue;
+    TreeNode c = p;
+    const int src = p.blank + move_delta(w, d);
+    c.board[p.blank] = p.board[src];
+    c.board[src] = 0;
+    c.blank = (uint8_t)src;
+    c.g = (uint8_t)(p.g + 1);
+    c.pre = (uint8_t)d;
+    c.move = (uint8_t)d;
+    c.parent = idx;
+    c.h = 0;
+    c.maxf = 0;
+    c.leaf = 1;
+    c.expanded = 0;
+    c.sub = -1;
+    tree.push_back(c);
+    ++cnt;
+  }
+  tree[idx].expanded = 1;
+  tree[idx].leaf = 0;
+  return cnt;
+}
+
+uint8_t count_children(int w, const TreeNode &t) {
+  uint32_t mv = legal_moves(w, t.blank);
+  if (t.pre != kNoPre) mv &= ~(1u << (3 - t.pre));
+  return (uint8_t)__builtin_popcount(mv);
+}
+
+// h for tree nodes [from, tree.size()) of every instance, on the GPU.
+int compute_tree_h(sp_solver *s, std::vector<Instance> &inst, const std::vector<size_t> &from) {
+  size_t total = 0;
+  for (size_t i = 0; i < inst.size(); ++i) total += inst[i].tree.size() - from[i];
+  if (!total) return SP_OK;
+  int rc = ensure(s, &s->d_boards, &s->boards_cap, total * (size_t)s->n);
+  if (rc) return rc;
+  rc = ensure(s, &s->d_h, &s->h_cap, total);
+  if (rc) return rc;
+  std::vector<uint8_t> boards(total * (size_t)s->n);
+  size_t o = 0;
+  for (size_t i = 0; i < inst.size(); ++i)
+    for (size_t j = from[i]; j < inst[i].tree.size(); ++j, ++o)
+      memcpy(&boards[o * s->n], inst[i].tree[j].board, (size_t)s->n);
+  SP_CUDA(s, cudaMemcpyAsync(s->d_boards, boards.data(), boards.size(), cudaMemcpyHostToDevice, s->st));
+  s->stats.h2d_bytes += boards.size();
+  SP_CUDA(s, launch_heuristic(s->w, s->heur == SP_HEUR_PDB, s->d_boards, (int)total, s->d_h, s->d_ht,
+                              s->d_pdb, s->st));
+  std::vector<int32_t> hv(total);
+  SP_CUDA(s, cudaMemcpyAsync(hv.data(), s->d_h, total * sizeof(int32_t), cudaMemcpyDeviceToHost, s->st));
+  SP_CUDA(s, cudaStreamSynchronize(s->st));
+  s->stats.d2h_bytes += total * sizeof(int32_t);
+  o = 0;
+  for (size_t i = 0; i < inst.size(); ++i)
+    for (size_t j = from[i]; j < inst[i].tree.size(); ++j, ++o) {
+      TreeNode &t = inst[i].tree[j];
+      t.h = hv[o];
+      const int f = (int)t.g + t.h;
+      t.maxf = t.parent < 0 ? f : std::max(inst[i].tree[t.parent].maxf, f);
+      t.nchild = count_children(s->w, t);
+    }
+  return SP_OK;
+}
+
+// Expand leaf `leaf` of an instance's tree breadth-first until it has at
+// least `pieces` leaves below it (or the depth budget runs out).
+void split_leaf(int w, Instance &I, int leaf, int pieces, int max_extra_depth) {
+  std::vector<int32_t> level{leaf};
+  for (int dep = 0; dep < max_extra_depth && (int)level.size() < pieces; ++dep) {
+    std::vector<int32_t> next;
+    for (int32_t x : level) {
+      size_t before = I.tree.size();
+      expand_node(w, I.tree, x);
+      for (size_t c = before; c < I.tree.size(); ++c) next.push_back((int32_t)c);
+    }
+    if (next.empty()) break;
+    level.swap(next);
+  }
+}
+
+void rebuild_leaves(Instance &I) {
+  I.leaves.clear();
+  for (size_t j = 0; j < I.tree.size(); ++j)
+    if (I.tree[j].leaf) I.leaves.push_back((int32_t)j);
+  I.last_load.assign(I.leaves.size(), 0);
+}
+
+bool replay_ok(int w, const uint8_t *tiles, const uint8_t *moves, int len) {
+  const int n = w * w;
+  uint8_t b[kMaxN];
+  int blank = 0;
+  for (int i = 0; i < n; ++i) {
+    b[i] = tiles[i];
+    if (!tiles[i]) blank = i;
+  }
+  for (int i = 0; i < len; ++i) {
+    if (moves[i] > 3 || !((legal_moves(w, blank) >> moves[i]) & 1u)) return false;
+    const int src = blank + move_delta(w, moves[i]);
+    b[blank] = b[src];
+    b[src] = 0;
+    blank = src;
+  }
+  for (int i = 0; i < n; ++i)
+    if (b[i] != i) return false;
+  return true;
+}
+
+int launch_round(sp_solver *s, uint32_t n_init, float *ms) {
+  ++s->stamp;
+  SP_CUDA(s, launch_pool_init(s->d_tasks, s->d_init, s->d_ready, n_init, s->stamp, s->d_ctl, s->st));
+  RoundParams P{};
+  P.subs = s->d_subs;
+  P.tasks = s->d_tasks;
+  P.ready = s->d_ready;
+  P.cap = s->cap;
+  P.stamp = s->stamp;
+  P.ctl = s->d_ctl;
+  P.inst_limit = s->d_limit;
+  P.sub_nodes = s->d_sub_nodes;
+  P.sol = s->d_sol;
+  P.ht = s->d_ht;
+  P.pdb = s->d_pdb;
+  P.min_slack = s->cfg.donate_min_slack;
+  P.steps = s->cfg.steps_per_poll;
+  P.donate = s->cfg.lb_mode == SP_LB_NONE ? 0 : 1;
+  P.timeout_ns = (unsigned long long)s->cfg.timeout_ms * 1000000ull;
+  const int block = s->cfg.threads_per_block == 128 ? 128 : 256;
+  SP_CUDA(s, cudaEventRecord(s->ev0, s->st));
+  int grid = 0;
+  SP_CUDA(s, launch_search_round(s->w, s->heur == SP_HEUR_PDB, block, s->cfg.blocks_per_sm, s->num_sms, P,
+                                 s->st, &grid));
+  SP_CUDA(s, cudaEventRecord(s->ev1, s->st));
+  SP_CUDA(s, cudaEventSynchronize(s->ev1));
+  SP_CUDA(s, cudaEventElapsedTime(ms, s->ev0, s->ev1));
+  s->stats.kernel_launches += 2;
+  s->last_grid = grid;
+  return SP_OK;
+}
+
+int ensure_pool(sp_solver *s, size_t n_init) {
+  size_t need = std::max<size_t>(n_init * 2 + 4096, (size_t)1 << 20);
+  if (s->cap >= need) return SP_OK;
+  if (s->d_tasks) cudaFree(s->d_tasks);
+  if (s->d_ready) cudaFree(s->d_ready);
+  s->d_tasks = nullptr;
+  s->d_ready = nullptr;
+  s->cap = 0;
+  SP_CUDA(s, cudaMalloc(&s->d_tasks, need * sizeof(Task)));
+  SP_CUDA(s, cudaMalloc(&s->d_ready, need * sizeof(uint32_t)));
+  SP_CUDA(s, cudaMemsetAsync(s->d_ready, 0, need * sizeof(uint32_t), s->st));
+  s->stamp = 0;
+  s->cap = (uint32_t)need;
+  return SP_OK;
+}
+
+int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
+  auto t_start = std::chrono::steady_clock::now();
+  memset(&s->stats, 0, sizeof(s->stats));
+  if (s->heur == SP_HEUR_PDB && !s->pdb_ready) {
+    s->err = "PDB heuristic selected but sp_pdb_build/sp_pdb_import not done";
+    return SP_ERR_NO_PDB;
+  }
+  const int w = s->w, n = s->n;
+  std::vector<Instance> inst((size_t)nin);
+  for (int i = 0; i < nin; ++i) {
+    Instance &I = inst[(size_t)i];
+    I.out = &res[i];
+    memset(I.out, 0, sizeof(sp_result));
+    I.out->len = -1;
+    I.status = check_instance(w, tiles + (size_t)i * n);
+    if (I.status != SP_OK) {
+      I.done = true;
+      I.out->status = I.status;
+      continue;
+    }
+    TreeNode root;
+    make_root(w, tiles + (size_t)i * n, &root);
+    I.tree.push_back(root);
+  }
+  // root set: uniform-depth tree expansion to >= frontier_target leaves
+  auto t_front = std::chrono::steady_clock::now();
+  const int target = std::max(1, s->cfg.frontier_target);
+  for (auto &I : inst) {
+    if (I.done) continue;
+    std::vector<int32_t> level{0};
+    I.tree[0].leaf = 1;
+    for (int dep = 0; dep < 40 && (int)level.size() < target; ++dep) {
+      std::vector<int32_t> next;
+      for (int32_t x : level) {
+        size_t before = I.tree.size();
+        expand_node(w, I.tree, x);
+        for (size_t c = before; c < I.tree.size(); ++c) next.push_back((int32_t)c);
+      }
+      level.swap(next);
+    }
+  }
+  std::vector<size_t> from(inst.size(), 0);
+  int rc = compute_tree_h(s, inst, from);
+  if (rc) return rc;
+  for (auto &I : inst) {
+    if (I.done) continue;
+    I.h0 = I.tree[0].h;
+    rebuild_leaves(I);
+  }
+  s->stats.frontier_ms += ms_since(t_front);
+
+  std::vector<int32_t> sub_base(inst.size(), 0);
+  std::vector<SubRoot> subs;
+  std::vector<Task> init;
+  std::vector<int32_t> limits(inst.size(), 0);
+  std::vector<unsigned long long> sub_nodes;
+  std::vector<Solution> sols(inst.size());
+  bool subs_dirty = true;
+
+  for (int round = 0; round < SP_MAX_ITERS; ++round) {
+    bool any = false;
+    for (auto &I : inst) any |= !I.done;
+    if (!any) break;
+    // (re)build the SubRoot array when the trees changed
+    if (subs_dirty) {
+      subs.clear();
+      for (size_t i = 0; i < inst.size(); ++i) {
+        sub_base[i] = (int32_t)subs.size();
+        Instance &I = inst[i];
+        if (I.done) continue;
+        for (int32_t x : I.leaves) {
+          TreeNode &t = I.tree[(size_t)x];
+          t.sub = (int32_t)subs.size();
+          SubRoot r{};
+          memcpy(r.board, t.board, (size_t)n);
+          r.blank = t.blank;
+          r.g = t.g;
+          r.pre = t.pre;
+          r.inst = (uint32_t)i;
+          subs.push_back(r);
+        }
+      }
+      rc = ensure(s, &s->d_subs, &s->subs_cap, std::max<size_t>(subs.size(), 1));
+      if (rc) return rc;
+      if (!subs.empty()) {
+        SP_CUDA(s, cudaMemcpyAsync(s->d_subs, subs.data(), subs.size() * sizeof(SubRoot),
+                                   cudaMemcpyHostToDevice, s->st));
+        s->stats.h2d_bytes += subs.size() * sizeof(SubRoot);
+      }
+      if (s->d_sub_nodes) cudaFree(s->d_sub_nodes);
+      s->d_sub_nodes = nullptr;
+      SP_CUDA(s, cudaMalloc(&s->d_sub_nodes, std::max<size_t>(subs.size(), 1) * sizeof(unsigned long long)));
+      subs_dirty = false;
+    }
+    // per instance: interior counts, host-side goals, active roots
+    init.clear();
+    std::vector<uint64_t> interior(inst.size(), 0);
+    std::vector<int32_t> host_goal(inst.size(), -1);
+    for (size_t i = 0; i < inst.size(); ++i) {
+      Instance &I = inst[i];
+      if (I.done) continue;
+      const int L = I.h0 + 2 * I.iter;
+      limits[i] = L;
+      for (size_t j = 0; j < I.tree.size(); ++j) {
+        const TreeNode &t = I.tree[j];
+        if (t.maxf > L) continue;
+        if (t.h == 0 && (host_goal[i] < 0 || t.g < I.tree[(size_t)host_goal[i]].g)) host_goal[i] = (int32_t)j;
+        if (!t.leaf) interior[i] += t.nchild;
+      }
+      for (int32_t x : I.leaves) {
+        const TreeNode &t = I.tree[(size_t)x];
+        if (t.maxf > L) continue;
+        Task tk{};
+        tk.sub = (uint32_t)t.sub;
+        tk.plen = 0;
+        tk.mask = 0xF;
+        init.push_back(tk);
+      }
+    }
+    // launch
+    rc = ensure_pool(s, init.size());
+    if (rc) return rc;
+    rc = ensure(s, &s->d_init, &s->init_cap, std::max<size_t>(init.size(), 1));
+    if (rc) return rc;
+    if (inst.size() > s->inst_cap || !s->d_limit) {
+      if (s->d_limit) cudaFree(s->d_limit);
+      if (s->d_sol) cudaFree(s->d_sol);
+      s->d_limit = nullptr;
+      s->d_sol = nullptr;
+      size_t c = std::max<size_t>(inst.size(), 64);
+      SP_CUDA(s, cudaMalloc(&s->d_limit, c * sizeof(int32_t)));
+      SP_CUDA(s, cudaMalloc(&s->d_sol, c * sizeof(Solution)));
+      s->inst_cap = c;
+    }
+    if (!init.empty()) {
+      SP_CUDA(s, cudaMemcpyAsync(s->d_init, init.data(), init.size() * sizeof(Task), cudaMemcpyHostToDevice, s->st));
+      s->stats.h2d_bytes += init.size() * sizeof(Task);
+    }
+    SP_CUDA(s, cudaMemcpyAsync(s->d_limit, limits.data(), inst.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s->st));
+    SP_CUDA(s, cudaMemsetAsync(s->d_sol, 0, inst.size() * sizeof(Solution), s->st));
+    SP_CUDA(s, cudaMemsetAsync(s->d_sub_nodes, 0, std::max<size_t>(subs.size(), 1) * sizeof(unsigned long long), s->st));
+    s->stats.h2d_bytes += inst.size() * sizeof(int32_t);
+    float ms = 0;
+    if (!init.empty()) {
+      rc = launch_round(s, (uint32_t)init.size(), &ms);
+      if (rc) return rc;
+      s->stats.kernel_ms += ms;
+      s->stats.tasks_initial += init.size();
+      PoolCtl ctl{};
+      SP_CUDA(s, cudaMemcpyAsync(&ctl, s->d_ctl, sizeof(PoolCtl), cudaMemcpyDeviceToHost, s->st));
+      sub_nodes.assign(subs.size(), 0);
+      SP_CUDA(s, cudaMemcpyAsync(sub_nodes.data(), s->d_sub_nodes, subs.size() * sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost, s->st));
+      SP_CUDA(s, cudaMemcpyAsync(sols.data(), s->d_sol, inst.size() * sizeof(Solution), cudaMemcpyDeviceToHost, s->st));
+      SP_CUDA(s, cudaStreamSynchronize(s->st));
+      s->stats.d2h_bytes += sizeof(PoolCtl) + subs.size() * 8 + inst.size() * sizeof(Solution);
+      s->stats.tasks_donated += ctl.donated;
+      if (ctl.error) {
+        char buf[160];
+        snprintf(buf, sizeof buf, "device error %d (info %u) in round %d", ctl.error, ctl.err_info[0], round);
+        s->err = buf;
+        for (auto &I : inst)
+          if (!I.done) { I.out->status = ctl.error; I.done = true; }
+        return ctl.error;
+      }
+    } else {
+      sub_nodes.assign(subs.size(), 0);
+      memset(sols.data(), 0, sols.size() * sizeof(Solution));
+    }
+    ++s->stats.rounds;
+    // fold results
+    for (size_t i = 0; i < inst.size(); ++i) {
+      Instance &I = inst[i];
+      if (I.done) continue;
+      uint64_t nodes = interior[i];
+      for (size_t q = 0; q < I.leaves.size(); ++q) {
+        const uint64_t v = sub_nodes[(size_t)I.tree[(size_t)I.leaves[q]].sub];
+        nodes += v;
+        I.last_load[q] = v;
+      }
+      sp_result *R = I.out;
+      R->f_limit[I.iter] = limits[i];
+      R->nodes[I.iter] = nodes;
+      R->nodes_total += nodes;
+      R->n_iter = I.iter + 1;
+      s->stats.nodes += nodes;
+      const bool dev_goal = sols[i].flag != 0;
+      if (host_goal[i] >= 0 || dev_goal) {
+        // path: root-set tree prefix, then the device's moves below its root
+        std::vector<uint8_t> mv;
+        int node = host_goal[i];
+        uint32_t extra = 0;
+        const uint32_t *pw = nullptr;
+        if (node < 0) {
+          const uint32_t sub = sols[i].sub;
+          for (int32_t x : I.leaves)
+            if (I.tree[(size_t)x].sub == (int32_t)sub) node = x;
+          extra = sols[i].len;
+          pw = sols[i].path;
+        }
+        for (int x = node; x > 0; x = I.tree[(size_t)x].parent) mv.push_back(I.tree[(size_t)x].move);
+        std::reverse(mv.begin(), mv.end());
+        for (uint32_t j = 0; j < extra; ++j) mv.push_back((uint8_t)((pw[j >> 4] >> (2 * (j & 15))) & 3u));
+        R->len = (int32_t)mv.size();
+        if (mv.size() > SP_MAX_MOVES) {
+          R->status = SP_ERR_PATH;
+        } else {
+          R->n_moves = R->len;
+          memcpy(R->moves, mv.data(), mv.size());
+          R->status = replay_ok(w, tiles + i * (size_t)n, R->moves, R->n_moves) ? SP_OK : SP_ERR_PATH;
+        }
+        I.done = true;
+        continue;
+      }
+      ++I.iter;
+      if (I.iter >= SP_MAX_ITERS) {
+        R->status = SP_ERR_LIMIT;
+        I.done = true;
+      }
+    }
+    // static load balancing: split heavy roots for the next round
+    if (s->cfg.lb_mode == SP_LB_STATIC_STEAL) {
+      std::vector<size_t> before(inst.size());
+      bool changed = false;
+      for (size_t i = 0; i < inst.size(); ++i) {
+        Instance &I = inst[i];
+        before[i] = I.tree.size();
+        if (I.done || I.leaves.empty()) continue;
+        uint64_t sum = 0;
+        for (uint64_t v : I.last_load) sum += v;
+        const uint64_t avg = sum / I.leaves.size();
+        if (!avg) continue;
+        const size_t cap_leaves = 65536;
+        for (size_t q = 0; q < I.leaves.size() && I.tree.size() < cap_leaves * 2; ++q) {
+          const uint64_t ld = I.last_load[q];
+          int pieces = (int)std::min<uint64_t>((ld - 1) / avg + 1, (uint64_t)std::max(2, s->cfg.static_split_cap));
+          if (ld > avg && pieces > 1) {
+            split_leaf(w, I, I.leaves[q], pieces, 8);
+            changed = true;
+          }
+        }
+      }
+      if (changed) {
+        rc = compute_tree_h(s, inst, before);
+        if (rc) return rc;
+        for (auto &I : inst)
+          if (!I.done) rebuild_leaves(I);
+        subs_dirty = true;
+      }
+    }
+  }
+  const double wall = ms_since(t_start);
+  for (auto &I : inst) {
+    I.out->seconds = wall / 1000.0;
+    if (!I.done && I.out->status == SP_OK) I.out->status = SP_ERR_LIMIT;
+  }
+  s->stats.wall_ms = wall;
+  return SP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void sp_config_default(sp_config *c) {
+  if (!c) return;
+  c->frontier_target = 2048;
+  c->threads_per_block = 256;
+  c->blocks_per_sm = 0;
+  c->lb_mode = SP_LB_STEAL;
+  c->donate_min_slack = 6;
+  c->steps_per_poll = 32;
+  c->timeout_ms = 20000;
+  c->static_split_cap = 64;
+}
+
+int sp_create(int width, int heuristic, const sp_config *cfg, sp_solver **out) {
+  if (!out || (width != 4 && width != 5) || (heuristic != SP_HEUR_MANHATTAN && heuristic != SP_HEUR_PDB))
+    return SP_ERR_ARG;
+  *out = nullptr;
+  std::unique_ptr<sp_solver> s(new sp_solver());
+  s->w = width;
+  s->n = width * width;
+  s->heur = heuristic;
+  sp_config_default(&s->cfg);
+  if (cfg) s->cfg = *cfg;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&s->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&s->ev1);
+  if (e == cudaSuccess) e = cudaMalloc(&s->d_ht, sizeof(HeurTables));
+  if (e == cudaSuccess) e = cudaMalloc(&s->d_ctl, sizeof(PoolCtl));
+  if (e == cudaSuccess) {
+    build_heur_tables(width, &s->h_ht);
+    e = cudaMemcpy(s->d_ht, &s->h_ht, sizeof(HeurTables), cudaMemcpyHostToDevice);
+  }
+  if (e == cudaSuccess && heuristic == SP_HEUR_PDB) {
+    const size_t bytes = (size_t)pattern_set(width).n_tables * lookup_table_stride(width);
+    e = cudaMalloc(&s->d_pdb, bytes);
+  }
+  if (e != cudaSuccess) {
+    sp_solver *raw = s.release();
+    raw->err = cudaGetErrorString(e);
+    sp_destroy(raw);
+    return SP_ERR_CUDA;
+  }
+  *out = s.release();
+  return SP_OK;
+}
+
+void sp_destroy(sp_solver *s) {
+  if (!s) return;
+  cudaFree(s->d_ht);
+  cudaFree(s->d_pdb);
+  cudaFree(s->d_tasks);
+  cudaFree(s->d_ready);
+  cudaFree(s->d_ctl);
+  cudaFree(s->d_subs);
+  cudaFree(s->d_init);
+  cudaFree(s->d_sub_nodes);
+  cudaFree(s->d_limit);
+  cudaFree(s->d_sol);
+  cudaFree(s->d_boards);
+  cudaFree(s->d_h);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  if (s->st) cudaStreamDestroy(s->st);
+  delete s;
+}
+
+int sp_set_config(sp_solver *s, const sp_config *cfg) {
+  if (!s || !cfg) return SP_ERR_ARG;
+  if (cfg->threads_per_block != 128 && cfg->threads_per_block != 256) return SP_ERR_ARG;
+  s->cfg = *cfg;
+  return SP_OK;
+}
+
+uint64_t sp_pdb_table_size(int width) {
+  if (width != 4 && width != 5) return 0;
+  return compact_table_size(width);
+}
+
+int sp_pdb_num_tables(int width) {
+  if (width != 4 && width != 5) return 0;
+  return pattern_set(width).n_tables;
+}
+
+int sp_pdb_build(sp_solver *s) {
+  if (!s) return SP_ERR_ARG;
+  if (s->heur != SP_HEUR_PDB) return SP_ERR_ARG;
+  const int nt = pattern_set(s->w).n_tables;
+  double total = 0;
+  for (int t = 0; t < nt; ++t) {
+    int levels = 0;
+    double ms = 0;
+    cudaError_t e = build_pdb_table(s->w, t, s->d_pdb + (size_t)t * lookup_table_stride(s->w), nullptr,
+                                    s->st, &levels, &ms);
+    if (e != cudaSuccess) return fail_cuda(s, e, "build_pdb_table");
+    total += ms;
+  }
+  s->pdb_build_ms = total;
+  s->pdb_ready = true;
+  return SP_OK;
+}
+
+int sp_pdb_export(sp_solver *s, int table, uint8_t *dst, uint64_t size) {
+  if (!s || !dst || s->heur != SP_HEUR_PDB) return SP_ERR_ARG;
+  if (table < 0 || table >= pattern_set(s->w).n_tables || size != compact_table_size(s->w)) return SP_ERR_ARG;
+  if (!s->pdb_ready) return SP_ERR_NO_PDB;
+  uint8_t *tmp = nullptr;
+  SP_CUDA(s, cudaMalloc(&tmp, size));
+  cudaError_t e = pdb_lookup_to_compact(s->w, table, s->d_pdb + (size_t)table * lookup_table_stride(s->w), tmp, s->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dst, tmp, size, cudaMemcpyDeviceToHost, s->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+  cudaFree(tmp);
+  if (e != cudaSuccess) return fail_cuda(s, e, "sp_pdb_export");
+  return SP_OK;
+}
+
+int sp_pdb_import(sp_solver *s, int table, const uint8_t *src, uint64_t size) {
+  if (!s || !src || s->heur != SP_HEUR_PDB) return SP_ERR_ARG;
+  const int nt = pattern_set(s->w).n_tables;
+  if (table < 0 || table >= nt || size != compact_table_size(s->w)) return SP_ERR_ARG;
+  uint8_t *tmp = nullptr;
+  SP_CUDA(s, cudaMalloc(&tmp, size));
+  cudaError_t e = cudaMemcpyAsync(tmp, src, size, cudaMemcpyHostToDevice, s->st);
+  if (e == cudaSuccess)
+    e = pdb_compact_to_lookup(s->w, table, tmp, s->d_pdb + (size_t)table * lookup_table_stride(s->w), s->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+  cudaFree(tmp);
+  if (e != cudaSuccess) return fail_cuda(s, e, "sp_pdb_import");
+  // tables become usable once every table has been imported or built
+  s->import_mask |= 1u << table;
+  if ((s->import_mask & ((1u << nt) - 1u)) == ((1u << nt) - 1u)) s->pdb_ready = true;
+  return SP_OK;
+}
+
+int sp_heuristic(sp_solver *s, const uint8_t *tiles, int n, int32_t *h) {
+  if (!s || (n > 0 && (!tiles || !h)) || n < 0) return SP_ERR_ARG;
+  if (s->heur == SP_HEUR_PDB && !s->pdb_ready) return SP_ERR_NO_PDB;
+  if (n == 0) return SP_OK;
+  for (int i = 0; i < n; ++i) {
+    int st = check_instance(s->w, tiles + (size_t)i * s->n);
+    if (st == SP_ERR_NOT_PERMUTATION) return st;
+  }
+  int rc = ensure(s, &s->d_boards, &s->boards_cap, (size_t)n * s->n);
+  if (rc) return rc;
+  int32_t *dh = nullptr;
+  SP_CUDA(s, cudaMalloc(&dh, (size_t)n * sizeof(int32_t)));
+  cudaError_t e = cudaMemcpyAsync(s->d_boards, tiles, (size_t)n * s->n, cudaMemcpyHostToDevice, s->st);
+  if (e == cudaSuccess) e = launch_heuristic(s->w, s->heur == SP_HEUR_PDB, s->d_boards, n, dh, s->d_ht, s->d_pdb, s->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, dh, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, s->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
+  cudaFree(dh);
+  if (e != cudaSuccess) return fail_cuda(s, e, "sp_heuristic");
+  return SP_OK;
+}
+
+int sp_solve_batch(sp_solver *s, const uint8_t *tiles, int n, sp_result *results) {
+  if (!s || n < 0 || (n > 0 && (!tiles || !results))) return SP_ERR_ARG;
+  if (n == 0) return SP_OK;
+  return solve_impl(s, tiles, n, results);
+}
+
+int sp_solve_batch_device(sp_solver *s, const void *d_tiles, int n, sp_result *results) {
+  if (!s || n < 0 || (n > 0 && (!d_tiles || !results))) return SP_ERR_ARG;
+  if (n == 0) return SP_OK;
+  std::vector<uint8_t> h((size_t)n * s->n);
+  SP_CUDA(s, cudaMemcpyAsync(h.data(), d_tiles, h.size(), cudaMemcpyDeviceToHost, s->st));
+  SP_CUDA(s, cudaStreamSynchronize(s->st));
+  int rc = solve_impl(s, h.data(), n, results);
+  s->stats.d2h_bytes += h.size();
+  return rc;
+}
+
+int sp_dfs_round(sp_solver *s, const uint8_t *roots, const int32_t *depth, const int32_t *pre, int n,
+                 int limit, uint64_t *nodes, int32_t *found) {
+  if (!s || n < 0 || (n > 0 && (!roots || !depth || !pre || !nodes)) || !found) return SP_ERR_ARG;
+  if (s->heur == SP_HEUR_PDB && !s->pdb_ready) return SP_ERR_NO_PDB;
+  memset(&s->stats, 0, sizeof(s->stats));
+  *found = -1;
+  if (n == 0) return SP_OK;
+  std::vector<SubRoot> subs((size_t)n);
+  std::vector<Task> init((size_t)n);
+  for (int i = 0; i < n; ++i) {
+    const uint8_t *t = roots + (size_t)i * s->n;
+    if (check_instance(s->w, t) == SP_ERR_NOT_PERMUTATION) return SP_ERR_NOT_PERMUTATION;
+    if (depth[i] < 0 || depth[i] > 255 || pre[i] < -1 || pre[i] > 3) return SP_ERR_ARG;
+    SubRoot r{};
+    memcpy(r.board, t, (size_t)s->n);
+    for (int c = 0; c < s->n; ++c)
+      if (!t[c]) r.blank = (uint8_t)c;
+    r.g = (uint8_t)depth[i];
+    r.pre = pre[i] < 0 ? kNoPre : (uint8_t)pre[i];
+    r.inst = 0;
+    subs[(size_t)i] = r;
+    init[(size_t)i].sub = (uint32_t)i;
+    init[(size_t)i].plen = 0;
+    init[(size_t)i].mask = 0xF;
+  }
+  // roots that are goals within the limit (the reference's dfs_kernel sets
+  // dev_flag for them, :580-583)
+  std::vector<int32_t> h((size_t)n);
+  int rc = sp_heuristic(s, roots, n, h.data());
+  if (rc) return rc;
+  for (int i = 0; i < n; ++i)
+    if (h[(size_t)i] == 0 && (*found < 0 || depth[i] < *found)) *found = depth[i];
+  rc = ensure(s, &s->d_subs, &s->subs_cap, (size_t)n);
+  if (rc) return rc;
+  rc = ensure(s, &s->d_init, &s->init_cap, (size_t)n);
+  if (rc) return rc;
+  rc = ensure_pool(s, (size_t)n);
+  if (rc) return rc;
+  if (!s->d_limit || s->inst_cap < 1) {
+    SP_CUDA(s, cudaMalloc(&s->d_limit, 64 * sizeof(int32_t)));
+    SP_CUDA(s, cudaMalloc(&s->d_sol, 64 * sizeof(Solution)));
+    s->inst_cap = 64;
+  }
+  if (s->d_sub_nodes) cudaFree(s->d_sub_nodes);
+  s->d_sub_nodes = nullptr;
+  SP_CUDA(s, cudaMalloc(&s->d_sub_nodes, (size_t)n * sizeof(unsigned long long)));
+  SP_CUDA(s, cudaMemcpyAsync(s->d_subs, subs.data(), subs.size() * sizeof(SubRoot), cudaMemcpyHostToDevice, s->st));
+  SP_CUDA(s, cudaMemcpyAsync(s->d_init, init.data(), init.size() * sizeof(Task), cudaMemcpyHostToDevice, s->st));
+  SP_CUDA(s, cudaMemcpyAsync(s->d_limit, &limit, sizeof(int32_t), cudaMemcpyHostToDevice, s->st));
+  SP_CUDA(s, cudaMemsetAsync(s->d_sol, 0, sizeof(Solution), s->st));
+  SP_CUDA(s, cudaMemsetAsync(s->d_sub_nodes, 0, (size_t)n * sizeof(unsigned long long), s->st));
+  float ms = 0;
+  rc = launch_round(s, (uint32_t)n, &ms);
+  if (rc) return rc;
+  PoolCtl ctl{};
+  Solution sol{};
+  SP_CUDA(s, cudaMemcpyAsync(&ctl, s->d_ctl, sizeof(PoolCtl), cudaMemcpyDeviceToHost, s->st));
+  SP_CUDA(s, cudaMemcpyAsync(&sol, s->d_sol, sizeof(Solution), cudaMemcpyDeviceToHost, s->st));
+  SP_CUDA(s, cudaMemcpyAsync(nodes, s->d_sub_nodes, (size_t)n * sizeof(uint64_t), cudaMemcpyDeviceToHost, s->st));
+  SP_CUDA(s, cudaStreamSynchronize(s->st));
+  s->stats.kernel_ms = ms;
+  s->stats.rounds = 1;
+  if (ctl.error) {
+    s->err = "device error in sp_dfs_round";
+    return ctl.error;
+  }
+  if (sol.flag) {
+    const int d = (int)subs[sol.sub].g + (int)sol.len;
+    if (*found < 0 || d < *found) *found = d;
+  }
+  for (int i = 0; i < n; ++i) s->stats.nodes += nodes[i];
+  return SP_OK;
+}
+
+int sp_last_stats(const sp_solver *s, sp_stats *out) {
+  if (!s || !out) return SP_ERR_ARG;
+  *out = s->stats;
+  return SP_OK;
+}
+
+const char *sp_status_string(int st) {
+  switch (st) {
+    case SP_OK: return "ok";
+    case SP_ERR_ARG: return "invalid argument";
+    case SP_ERR_NOT_PERMUTATION: return "tiles are not a permutation";
+    case SP_ERR_UNSOLVABLE: return "instance is unsolvable";
+    case SP_ERR_LIMIT: return "no solution within the threshold cap";
+    case SP_ERR_CUDA: return "CUDA error";
+    case SP_ERR_NO_PDB: return "pattern databases not built";
+    case SP_ERR_STACK_OVERFLOW: return "search deeper than the per-lane stack";
+    case SP_ERR_TIMEOUT: return "device wait timed out";
+    case SP_ERR_CAPACITY: return "capacity exceeded";
+    case SP_ERR_PATH: return "solution path invalid or too long";
+  }
+  return "unknown status";
+}
+
+const char *sp_last_error(const sp_solver *s) { return s ? s->err.c_str() : "null solver"; }
+
+uint64_t sp_kernel_launch_count(void) { return g_launches.load(); }
+
+}  // extern "C"

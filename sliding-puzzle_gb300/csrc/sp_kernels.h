@@ -1,0 +1,58 @@
+// Kernel interfaces of libslide (device side), used by the host round loop.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sp_defs.h"
+
+namespace sp {
+
+struct RoundParams {
+  const SubRoot *subs;
+  Task *tasks;
+  uint32_t *ready;          // ready[slot] == stamp once tasks[slot] is published
+  uint32_t cap;             // pool capacity (slots)
+  uint32_t stamp;
+  PoolCtl *ctl;
+  const int32_t *inst_limit;
+  unsigned long long *sub_nodes;
+  Solution *sol;
+  const HeurTables *ht;
+  const uint8_t *pdb;       // device tables, table t at t << (w == 4 ? 20 : 28)
+  int32_t min_slack;
+  int32_t steps;
+  int32_t donate;
+  int32_t pad;
+  unsigned long long timeout_ns;
+};
+
+// One threshold round: grid = num_sms * blocks_per_sm (0 = occupancy maximum).
+cudaError_t launch_search_round(int w, bool pdb, int block, int blocks_per_sm, int num_sms,
+                                const RoundParams &P, cudaStream_t st, int *grid_out);
+// Publish the round's first n tasks and reset the pool control block.
+cudaError_t launch_pool_init(Task *tasks, const Task *init, uint32_t *ready, uint32_t n,
+                             uint32_t stamp, PoolCtl *ctl, cudaStream_t st);
+
+// h of n boards (n * N bytes) into h[n]; PDB tables as in RoundParams.
+cudaError_t launch_heuristic(int w, bool pdb, const uint8_t *boards, int n, int32_t *h,
+                             const HeurTables *ht, const uint8_t *tables, cudaStream_t st);
+
+// Breadth-first build of table `table_id` of width w into the device lookup
+// layout (mixed radix 16^5 or 25^6 bytes) at `lookup`; also writes the
+// compact rank-order table to `compact` when non-null.  Scratch is allocated
+// and freed inside.
+cudaError_t build_pdb_table(int w, int table_id, uint8_t *lookup, uint8_t *compact,
+                            cudaStream_t st, int *levels_out, double *ms_out);
+// compact rank order <-> lookup layout
+cudaError_t pdb_compact_to_lookup(int w, int table_id, const uint8_t *compact, uint8_t *lookup,
+                                  cudaStream_t st);
+cudaError_t pdb_lookup_to_compact(int w, int table_id, const uint8_t *lookup, uint8_t *compact,
+                                  cudaStream_t st);
+
+uint64_t compact_table_size(int w);
+uint64_t lookup_table_stride(int w);
+
+// launch counter shared by all translation units
+void note_launch(int n = 1);
+
+}  // namespace sp

@@ -1,0 +1,258 @@
+"""Python binding of libslide (include/slide.h) over ctypes.
+
+Mirrors the reference's solver interface -- state in, optimal move sequence
+and per-iteration node counts out (src/24puzzle_expand.cc:146-164 prints
+`len node_num`; src/24puzzle_block_parallel_with_pdb.cu:756-922 solves one
+instance per call) -- for batches of instances on one GPU.  There is no CPU
+search path: loading fails loudly when libslide.so is missing, and creating
+a solver fails when no GPU is usable.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libslide.so")
+
+SP_MAX_ITERS = 96
+SP_MAX_MOVES = 240
+HEUR = {"manhattan": 0, "md": 0, "pdb": 1}
+LB = {"steal": 0, "static": 1, "static_steal": 1, "none": 2}
+MOVE_NAMES = "URLD"  # blank moves: 0 up, 1 right, 2 left, 3 down
+
+
+class SlideError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s (status %d)" % (msg, status))
+        self.status = status
+
+
+class SpConfig(ctypes.Structure):
+    _fields_ = [("frontier_target", ctypes.c_int32), ("threads_per_block", ctypes.c_int32),
+                ("blocks_per_sm", ctypes.c_int32), ("lb_mode", ctypes.c_int32),
+                ("donate_min_slack", ctypes.c_int32), ("steps_per_poll", ctypes.c_int32),
+                ("timeout_ms", ctypes.c_int32), ("static_split_cap", ctypes.c_int32)]
+
+
+class SpResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("len", ctypes.c_int32), ("n_iter", ctypes.c_int32),
+                ("n_moves", ctypes.c_int32), ("nodes_total", ctypes.c_uint64),
+                ("f_limit", ctypes.c_int32 * SP_MAX_ITERS), ("nodes", ctypes.c_uint64 * SP_MAX_ITERS),
+                ("moves", ctypes.c_uint8 * SP_MAX_MOVES), ("seconds", ctypes.c_double)]
+
+
+class SpStats(ctypes.Structure):
+    _fields_ = [("frontier_ms", ctypes.c_double), ("kernel_ms", ctypes.c_double), ("wall_ms", ctypes.c_double),
+                ("rounds", ctypes.c_int32), ("kernel_launches", ctypes.c_int32),
+                ("tasks_initial", ctypes.c_uint64), ("tasks_donated", ctypes.c_uint64),
+                ("nodes", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]
+
+
+_lib = None
+
+
+def load(build=True):
+    """Load libslide.so (building it first when `build` and sources changed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build:
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("slide_build", os.path.join(HERE, "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+    if not os.path.exists(LIB_PATH):
+        raise OSError("libslide.so not built: %s" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    P, I32, U64 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_uint64
+    sig = {
+        "sp_config_default": (None, [ctypes.POINTER(SpConfig)]),
+        "sp_create": (I32, [I32, I32, ctypes.POINTER(SpConfig), ctypes.POINTER(P)]),
+        "sp_destroy": (None, [P]),
+        "sp_set_config": (I32, [P, ctypes.POINTER(SpConfig)]),
+        "sp_pdb_build": (I32, [P]),
+        "sp_pdb_table_size": (U64, [I32]),
+        "sp_pdb_num_tables": (I32, [I32]),
+        "sp_pdb_export": (I32, [P, I32, P, U64]),
+        "sp_pdb_import": (I32, [P, I32, P, U64]),
+        "sp_heuristic": (I32, [P, P, I32, P]),
+        "sp_solve_batch": (I32, [P, P, I32, ctypes.POINTER(SpResult)]),
+        "sp_solve_batch_device": (I32, [P, P, I32, ctypes.POINTER(SpResult)]),
+        "sp_dfs_round": (I32, [P, P, P, P, I32, I32, P, P]),
+        "sp_last_stats": (I32, [P, ctypes.POINTER(SpStats)]),
+        "sp_status_string": (ctypes.c_char_p, [I32]),
+        "sp_last_error": (ctypes.c_char_p, [P]),
+        "sp_kernel_launch_count": (U64, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def default_config(**overrides):
+    lib = load()
+    cfg = SpConfig()
+    lib.sp_config_default(ctypes.byref(cfg))
+    for k, v in overrides.items():
+        if k == "lb_mode" and isinstance(v, str):
+            v = LB[v]
+        setattr(cfg, k, int(v))
+    return cfg
+
+
+def _as_tiles(tiles, width):
+    a = np.ascontiguousarray(np.asarray(tiles, dtype=np.uint8))
+    if a.ndim == 1:
+        a = a.reshape(1, -1)
+    if a.ndim != 2 or a.shape[1] != width * width:
+        raise ValueError("tiles must have shape (n, %d)" % (width * width))
+    return a
+
+
+class Solver:
+    """One GPU solver (one CUDA stream, device memory owned by the handle)."""
+
+    def __init__(self, width, heuristic="manhattan", config=None, **overrides):
+        self.lib = load()
+        self.width = int(width)
+        self.heuristic = heuristic
+        cfg = config if config is not None else default_config(**overrides)
+        h = ctypes.c_void_p()
+        st = self.lib.sp_create(self.width, HEUR[heuristic], ctypes.byref(cfg), ctypes.byref(h))
+        if st != 0:
+            raise SlideError(st, "sp_create failed: %s" % self.lib.sp_status_string(st).decode())
+        self.h = h
+        self.config = cfg
+
+    def _check(self, st, what):
+        if st != 0:
+            msg = self.lib.sp_last_error(self.h).decode() or self.lib.sp_status_string(st).decode()
+            raise SlideError(st, "%s: %s" % (what, msg))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_config(self, **overrides):
+        cfg = SpConfig.from_buffer_copy(self.config)
+        for k, v in overrides.items():
+            if k == "lb_mode" and isinstance(v, str):
+                v = LB[v]
+            setattr(cfg, k, int(v))
+        self._check(self.lib.sp_set_config(self.h, ctypes.byref(cfg)), "sp_set_config")
+        self.config = cfg
+
+    # --- pattern databases ---
+    def build_pdb(self):
+        self._check(self.lib.sp_pdb_build(self.h), "sp_pdb_build")
+
+    def table_size(self):
+        return int(self.lib.sp_pdb_table_size(self.width))
+
+    def num_tables(self):
+        return int(self.lib.sp_pdb_num_tables(self.width))
+
+    def export_pdb(self, table):
+        out = np.empty(self.table_size(), dtype=np.uint8)
+        self._check(self.lib.sp_pdb_export(self.h, table, out.ctypes.data, out.size), "sp_pdb_export")
+        return out
+
+    def import_pdb(self, table, data):
+        a = np.ascontiguousarray(np.asarray(data, dtype=np.uint8))
+        self._check(self.lib.sp_pdb_import(self.h, table, a.ctypes.data, a.size), "sp_pdb_import")
+
+    # --- search ---
+    def heuristic_values(self, tiles):
+        a = _as_tiles(tiles, self.width)
+        out = np.empty(a.shape[0], dtype=np.int32)
+        self._check(self.lib.sp_heuristic(self.h, a.ctypes.data, a.shape[0], out.ctypes.data), "sp_heuristic")
+        return out
+
+    def solve_raw(self, tiles):
+        a = _as_tiles(tiles, self.width)
+        res = (SpResult * max(1, a.shape[0]))()
+        self._check(self.lib.sp_solve_batch(self.h, a.ctypes.data, a.shape[0], res), "sp_solve_batch")
+        return res
+
+    def solve(self, tiles):
+        """Solve a batch; returns one dict per instance."""
+        return [result_dict(r) for r in self.solve_raw(tiles)[: _as_tiles(tiles, self.width).shape[0]]]
+
+    def solve_device_raw(self, dev_ptr, n):
+        res = (SpResult * max(1, n))()
+        self._check(self.lib.sp_solve_batch_device(self.h, ctypes.c_void_p(dev_ptr), n, res),
+                    "sp_solve_batch_device")
+        return res
+
+    def dfs_round(self, roots, depth, pre, limit):
+        """One threshold round over a root set (the reference's dfs_kernel)."""
+        a = _as_tiles(roots, self.width)
+        n = a.shape[0]
+        d = np.ascontiguousarray(np.asarray(depth, dtype=np.int32).reshape(n))
+        p = np.ascontiguousarray(np.asarray(pre, dtype=np.int32).reshape(n))
+        nodes = np.zeros(n, dtype=np.uint64)
+        found = ctypes.c_int32(-1)
+        self._check(self.lib.sp_dfs_round(self.h, a.ctypes.data, d.ctypes.data, p.ctypes.data, n, int(limit),
+                                          nodes.ctypes.data, ctypes.byref(found)), "sp_dfs_round")
+        return nodes, int(found.value)
+
+    def stats(self):
+        s = SpStats()
+        self._check(self.lib.sp_last_stats(self.h, ctypes.byref(s)), "sp_last_stats")
+        return {f: getattr(s, f) for f, _ in SpStats._fields_}
+
+
+def result_dict(r):
+    n = r.n_iter
+    return {
+        "status": int(r.status),
+        "len": int(r.len),
+        "n_iter": int(n),
+        "f_limit": [int(x) for x in r.f_limit[:n]],
+        "nodes": [int(x) for x in r.nodes[:n]],
+        "nodes_total": int(r.nodes_total),
+        "moves": bytes(r.moves[: r.n_moves]),
+        "seconds": float(r.seconds),
+    }
+
+
+def kernel_launch_count():
+    return int(load().sp_kernel_launch_count())
+
+
+def replay(tiles, moves, width):
+    """Apply blank moves to a state; returns the final state (numpy)."""
+    b = np.array(tiles, dtype=np.uint8).reshape(-1).copy()
+    blank = int(np.flatnonzero(b == 0)[0])
+    delta = (-width, 1, -1, width)
+    for m in moves:
+        r, c = divmod(blank, width)
+        ok = (m == 0 and r > 0) or (m == 1 and c < width - 1) or (m == 2 and c > 0) or (m == 3 and r < width - 1)
+        if not ok:
+            raise ValueError("illegal move %d at blank %d" % (m, blank))
+        src = blank + delta[m]
+        b[blank], b[src] = b[src], 0
+        blank = src
+    return b
+
+
+def is_solution(tiles, moves, width):
+    return bool(np.array_equal(replay(tiles, moves, width), np.arange(width * width, dtype=np.uint8)))
