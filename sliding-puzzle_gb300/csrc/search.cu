@@ -232,6 +232,10 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
     limit = P.inst_limit[inst];
     for (int i = 0; i < plen; ++i) {
       int d = task_dir(i);
+      if (!((legal_moves(W, blank) >> d) & 1u)) {  // corrupt record: never index off the board
+        set_error(SP_ERR_ARG, 0x100u + (uint32_t)i);
+        return false;
+      }
       int src = blank + move_delta(W, d);
       slide(tile_at(src), src, blank);
       blank = src;
@@ -406,7 +410,7 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
       out = __shfl_sync(FULL, out, 0);
       err = __shfl_sync(FULL, err, 0);
       if (out == 0 || err != 0) break;
-      __nanosleep(500);
+      __nanosleep(1000);
       continue;
     }
     // 4. search

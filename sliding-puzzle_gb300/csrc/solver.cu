@@ -628,6 +628,14 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
   return SP_OK;
 }
 
+bool config_ok(const sp_config *c) {
+  return (c->threads_per_block == 128 || c->threads_per_block == 256) && c->frontier_target >= 1 &&
+         c->frontier_target <= (1 << 20) && c->blocks_per_sm >= 0 && c->blocks_per_sm <= 16 &&
+         c->lb_mode >= SP_LB_STEAL && c->lb_mode <= SP_LB_NONE && c->donate_min_slack >= 0 &&
+         c->steps_per_poll >= 1 && c->steps_per_poll <= 4096 && c->timeout_ms >= 100 &&
+         c->timeout_ms <= 600000 && c->static_split_cap >= 1;
+}
+
 }  // namespace
 
 extern "C" {
@@ -648,6 +656,7 @@ int sp_create(int width, int heuristic, const sp_config *cfg, sp_solver **out) {
   if (!out || (width != 4 && width != 5) || (heuristic != SP_HEUR_MANHATTAN && heuristic != SP_HEUR_PDB))
     return SP_ERR_ARG;
   *out = nullptr;
+  if (cfg && !config_ok(cfg)) return SP_ERR_ARG;
   std::unique_ptr<sp_solver> s(new sp_solver());
   s->w = width;
   s->n = width * width;
@@ -701,8 +710,7 @@ void sp_destroy(sp_solver *s) {
 }
 
 int sp_set_config(sp_solver *s, const sp_config *cfg) {
-  if (!s || !cfg) return SP_ERR_ARG;
-  if (cfg->threads_per_block != 128 && cfg->threads_per_block != 256) return SP_ERR_ARG;
+  if (!s || !cfg || !config_ok(cfg)) return SP_ERR_ARG;
   s->cfg = *cfg;
   return SP_OK;
 }
