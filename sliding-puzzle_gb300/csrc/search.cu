@@ -98,6 +98,7 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
   __shared__ uint8_t s_pat[PDB ? 2 * N : 1];
   __shared__ int8_t s_mdd[PDB ? 1 : 4 * N * N];
   __shared__ uint32_t s_stack[WORDS][BLOCK];
+  __shared__ uint32_t s_prefix[kPathWords][BLOCK];  // the lane's task prefix (its pool slot is freed)
   __shared__ __align__(16) uint8_t s_board[W == 5 ? BLOCK * BSTRIDE : 4];
 
   const HeurTables *ht = P.ht;
@@ -156,8 +157,7 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
     return (int)((w >> (2 * (i & 15))) & 3u);
   };
   auto task_dir = [&](int i) -> int {
-    uint32_t w = __ldcg(&P.tasks[slot].path[i >> 4]);
-    return (int)((w >> (2 * (i & 15))) & 3u);
+    return (int)((s_prefix[i >> 4][tid] >> (2 * (i & 15))) & 3u);
   };
   // moves 0..len-1 of the lane's path below its SubRoot: task prefix then stack
   auto path_word = [&](int wi, int len) -> uint32_t {
@@ -207,12 +207,20 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
     atomicSub(&ctl->outstanding, 1u);
     state = 0;
   };
-  auto start_task = [&]() -> bool {
-    const Task *T = &P.tasks[slot];
+  // Copy the claimed record out of its ring slot, then free the slot for the
+  // producer of index slot + cap.
+  auto take_task = [&]() {
+    const uint32_t s = slot & (P.cap - 1u);
+    const Task *T = &P.tasks[s];
     sub = __ldcg(&T->sub);
-    uint32_t hdr = __ldcg((const uint32_t *)T + 1);
+    const uint32_t hdr = __ldcg((const uint32_t *)T + 1);
     plen = (int)(hdr & 0xFFFFu);
     mask0 = (hdr >> 16) & 0xFu;
+    for (int wi = 0; wi < kPathWords; ++wi) s_prefix[wi][tid] = __ldcg(&T->path[wi]);
+    __threadfence();
+    atomicExch(&P.seq[s], slot + P.cap);
+  };
+  auto start_task = [&]() -> bool {
     const SubRoot *R = &P.subs[sub];
     const uint8_t *rb = R->board;
     if (W == 4) {
@@ -382,9 +390,10 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
         state = 1;
       }
     }
-    // 2. a claimed slot becomes a task once its producer published it
-    if (state == 1 && slot < P.cap && ld_volatile(&P.ready[slot]) == P.stamp) {
+    // 2. a claimed index becomes a task once its producer published it
+    if (state == 1 && ld_volatile(&P.seq[slot & (P.cap - 1u)]) == slot + 1u) {
       __threadfence();
+      take_task();
       if (start_task()) state = 2;
       else finish_task();
     }
@@ -434,24 +443,28 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
     tl = __shfl_sync(FULL, tl, 0);
     err = __shfl_sync(FULL, err, 0);
     if (err) break;
-    if (P.donate && hd > tl && tl < P.cap) {
+    if (P.donate && hd > tl) {
       uint32_t dmask = 0;
       int lev = (state == 2) ? find_donation(dmask) : -1;
+      if (lev >= 0 && plen + lev > kMaxPath) lev = -1;  // prefix would not fit a record
       // one donor per warp per poll: the lane with the shallowest level
       const unsigned key = lev >= 0 ? ((unsigned)lev << 5) | (unsigned)lane : 0xFFFFFFFFu;
       const unsigned best = __reduce_min_sync(FULL, key);
       if (best != 0xFFFFFFFFu && (int)(best & 31u) == lane) {
+        // reserve index t only while someone waits for it (t < head) and its
+        // ring slot is free (its previous occupant, t - cap, was taken)
+        const uint32_t mask = P.cap - 1u;
         uint32_t t = ld_volatile(&ctl->tail), hh = ld_volatile(&ctl->head);
         bool ok = false;
-        while (t < hh && t < P.cap) {
+        while (t < hh && ld_volatile(&P.seq[t & mask]) == t) {
           const uint32_t old = atomicCAS(&ctl->tail, t, t + 1);
           if (old == t) { ok = true; break; }
           t = old;
           hh = ld_volatile(&ctl->head);
         }
-        if (ok && plen + lev <= kMaxPath) {
+        if (ok) {
           atomicAdd(&ctl->outstanding, 1u);
-          Task *D = &P.tasks[t];
+          Task *D = &P.tasks[t & mask];
           const int nlen = plen + lev;
           D->sub = sub;
           D->plen = (uint16_t)nlen;
@@ -459,33 +472,26 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
           D->flags = 1;
           for (int wi = 0; wi < kPathWords; ++wi) D->path[wi] = path_word(wi, nlen);
           __threadfence();
-          atomicExch(&P.ready[t], P.stamp);
+          atomicExch(&P.seq[t & mask], t + 1u);
           atomicAdd(&ctl->donated, 1ull);
           if (lev == k) it = 4;
           else cut |= 1ull << lev;
-        } else if (ok) {
-          // cannot encode the prefix: publish an empty task so the slot's claimant moves on
-          atomicAdd(&ctl->outstanding, 1u);
-          Task *D = &P.tasks[t];
-          D->sub = sub;
-          D->plen = 0;
-          D->mask = 0;
-          D->flags = 2;
-          __threadfence();
-          atomicExch(&P.ready[t], P.stamp);
         }
       }
     }
   }
 }
 
-// Fill the first n pool slots with the round's root tasks and publish them.
-__global__ void pool_init_kernel(Task *tasks, const Task *init, uint32_t *ready, uint32_t n,
-                                 uint32_t stamp, PoolCtl *ctl) {
+// Reset the ring (seq[s] = s: slot s free for index s), fill indices [0, n)
+// with the round's root tasks and publish them (seq = index + 1).
+__global__ void pool_init_kernel(Task *tasks, const Task *init, uint32_t *seq, uint32_t n, uint32_t cap,
+                                 PoolCtl *ctl) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
     tasks[i] = init[i];
-    ready[i] = stamp;
+    seq[i] = i + 1u;
+  } else if (i < cap) {
+    seq[i] = i;
   }
   if (i == 0) {
     ctl->head = 0;
@@ -526,10 +532,10 @@ cudaError_t launch_search_round(int w, bool pdb, int block, int blocks_per_sm, i
   return cudaGetLastError();
 }
 
-cudaError_t launch_pool_init(Task *tasks, const Task *init, uint32_t *ready, uint32_t n,
-                             uint32_t stamp, PoolCtl *ctl, cudaStream_t st) {
-  const uint32_t blocks = n ? (n + 255) / 256 : 1;
-  pool_init_kernel<<<blocks, 256, 0, st>>>(tasks, init, ready, n, stamp, ctl);
+cudaError_t launch_pool_init(Task *tasks, const Task *init, uint32_t *seq, uint32_t n, uint32_t cap,
+                             PoolCtl *ctl, cudaStream_t st) {
+  const uint32_t blocks = (cap + 255) / 256;
+  pool_init_kernel<<<blocks, 256, 0, st>>>(tasks, init, seq, n, cap, ctl);
   note_launch();
   return cudaGetLastError();
 }

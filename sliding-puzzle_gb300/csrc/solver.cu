@@ -111,7 +111,7 @@ struct sp_solver {
   int last_grid = 0;
   // device task pool
   Task *d_tasks = nullptr;
-  uint32_t *d_ready = nullptr;
+  uint32_t *d_seq = nullptr;
   uint32_t cap = 0;
   PoolCtl *d_ctl = nullptr;
   uint32_t stamp = 0;
@@ -321,14 +321,12 @@ bool replay_ok(int w, const uint8_t *tiles, const uint8_t *moves, int len) {
 }
 
 int launch_round(sp_solver *s, uint32_t n_init, float *ms) {
-  ++s->stamp;
-  SP_CUDA(s, launch_pool_init(s->d_tasks, s->d_init, s->d_ready, n_init, s->stamp, s->d_ctl, s->st));
+  SP_CUDA(s, launch_pool_init(s->d_tasks, s->d_init, s->d_seq, n_init, s->cap, s->d_ctl, s->st));
   RoundParams P{};
   P.subs = s->d_subs;
   P.tasks = s->d_tasks;
-  P.ready = s->d_ready;
+  P.seq = s->d_seq;
   P.cap = s->cap;
-  P.stamp = s->stamp;
   P.ctl = s->d_ctl;
   P.inst_limit = s->d_limit;
   P.sub_nodes = s->d_sub_nodes;
@@ -352,18 +350,23 @@ int launch_round(sp_solver *s, uint32_t n_init, float *ms) {
   return SP_OK;
 }
 
+// Ring capacity: a power of two holding the round's root tasks plus room for
+// a waiting claim from every resident lane.
 int ensure_pool(sp_solver *s, size_t n_init) {
-  size_t need = std::max<size_t>(n_init * 2 + 4096, (size_t)1 << 20);
+  size_t need = (size_t)1 << 20;
+  while (need < n_init + ((size_t)1 << 19)) need <<= 1;
+  if (need > ((size_t)1 << 30)) {
+    s->err = "too many root tasks for the task pool";
+    return SP_ERR_CAPACITY;
+  }
   if (s->cap >= need) return SP_OK;
   if (s->d_tasks) cudaFree(s->d_tasks);
-  if (s->d_ready) cudaFree(s->d_ready);
+  if (s->d_seq) cudaFree(s->d_seq);
   s->d_tasks = nullptr;
-  s->d_ready = nullptr;
+  s->d_seq = nullptr;
   s->cap = 0;
   SP_CUDA(s, cudaMalloc(&s->d_tasks, need * sizeof(Task)));
-  SP_CUDA(s, cudaMalloc(&s->d_ready, need * sizeof(uint32_t)));
-  SP_CUDA(s, cudaMemsetAsync(s->d_ready, 0, need * sizeof(uint32_t), s->st));
-  s->stamp = 0;
+  SP_CUDA(s, cudaMalloc(&s->d_seq, need * sizeof(uint32_t)));
   s->cap = (uint32_t)need;
   return SP_OK;
 }
@@ -694,7 +697,7 @@ void sp_destroy(sp_solver *s) {
   cudaFree(s->d_ht);
   cudaFree(s->d_pdb);
   cudaFree(s->d_tasks);
-  cudaFree(s->d_ready);
+  cudaFree(s->d_seq);
   cudaFree(s->d_ctl);
   cudaFree(s->d_subs);
   cudaFree(s->d_init);

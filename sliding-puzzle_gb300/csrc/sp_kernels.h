@@ -9,10 +9,13 @@ namespace sp {
 
 struct RoundParams {
   const SubRoot *subs;
+  // Task pool: a ring of `cap` slots (a power of two).  Index i lives in slot
+  // i & (cap-1); seq[slot] == i once the slot is free for index i, == i + 1
+  // once index i is published, and becomes i + cap when its claimant copied it.
   Task *tasks;
-  uint32_t *ready;          // ready[slot] == stamp once tasks[slot] is published
-  uint32_t cap;             // pool capacity (slots)
-  uint32_t stamp;
+  uint32_t *seq;
+  uint32_t cap;
+  uint32_t pad0;
   PoolCtl *ctl;
   const int32_t *inst_limit;
   unsigned long long *sub_nodes;
@@ -30,8 +33,8 @@ struct RoundParams {
 cudaError_t launch_search_round(int w, bool pdb, int block, int blocks_per_sm, int num_sms,
                                 const RoundParams &P, cudaStream_t st, int *grid_out);
 // Publish the round's first n tasks and reset the pool control block.
-cudaError_t launch_pool_init(Task *tasks, const Task *init, uint32_t *ready, uint32_t n,
-                             uint32_t stamp, PoolCtl *ctl, cudaStream_t st);
+cudaError_t launch_pool_init(Task *tasks, const Task *init, uint32_t *seq, uint32_t n, uint32_t cap,
+                             PoolCtl *ctl, cudaStream_t st);
 
 // h of n boards (n * N bytes) into h[n]; PDB tables as in RoundParams.
 cudaError_t launch_heuristic(int w, bool pdb, const uint8_t *boards, int n, int32_t *h,

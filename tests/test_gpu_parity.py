@@ -99,7 +99,7 @@ def test_pdb24_golden_all_rows(gpu_solver, gpu_tables):
 @pytest.mark.parametrize("lb", ["steal", "static", "none"])
 def test_load_balance_modes_keep_counts(gpu_solver, lb):
     s = gpu_solver(4, "manhattan")
-    states = instances.random_permutations(4, 12, seed=21)[:6]
+    states = instances.random_walks(4, 24, (60, 90), seed=21)
     want = oracle.solve(4, states, oracle.MD)
     s.set_config(lb_mode=lb, frontier_target=256 if lb != "none" else 2048)
     got = s.solve(states)
