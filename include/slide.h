@@ -92,6 +92,8 @@ typedef struct {
   double seconds;            /* wall time of the batch this instance was in */
 } sp_result;
 
+#define SP_MAX_ROUNDS 96
+
 typedef struct {
   double frontier_ms;        /* host root-set construction */
   double kernel_ms;          /* device time of the round kernels (events) */
@@ -102,6 +104,18 @@ typedef struct {
   uint64_t tasks_donated;    /* tasks created by in-kernel donation */
   uint64_t nodes;            /* generated nodes, all instances, all rounds */
   uint64_t h2d_bytes, d2h_bytes;
+  /* per threshold round of the batch */
+  int32_t round_instances[SP_MAX_ROUNDS];  /* unsolved instances searched */
+  int32_t round_tasks[SP_MAX_ROUNDS];      /* root tasks published */
+  float round_kernel_ms[SP_MAX_ROUNDS];
+  float round_host_ms[SP_MAX_ROUNDS];      /* host work of the round */
+  uint64_t round_nodes[SP_MAX_ROUNDS];
+  uint64_t round_donated[SP_MAX_ROUNDS];
+  /* search-kernel efficiency, summed over rounds */
+  uint64_t dev_lane_steps;   /* DFS steps executed by lanes */
+  uint64_t dev_lane_slots;   /* lane slots offered by warps' step loops */
+  uint64_t dev_idle_cycles;  /* warp cycles with no lane searching */
+  uint64_t dev_warp_cycles;  /* all warp cycles */
 } sp_stats;
 
 typedef struct sp_solver sp_solver;

@@ -25,6 +25,7 @@
 #include <chrono>
 
 #include "sp_defs.h"
+#include "sp_device.cuh"
 #include "sp_kernels.h"
 
 namespace sp {
@@ -193,34 +194,7 @@ __global__ void heuristic_kernel(const uint8_t *boards, int n, int32_t *hout, co
   constexpr int N = W * W;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const uint8_t *b = boards + (size_t)i * N;
-  if (!PDB) {
-    int s = 0;
-    for (int c = 0; c < N; ++c) {
-      int t = b[c];
-      if (!t) continue;
-      s += abs(c / W - t / W) + abs(c % W - t % W);
-    }
-    hout[i] = s;
-    return;
-  }
-  constexpr int NP = W == 5 ? 4 : 3;
-  uint32_t idx[2][4] = {{0, 0, 0, 0}, {0, 0, 0, 0}};
-  for (int c = 0; c < N; ++c) {
-    int t = b[c];
-    if (!t) continue;
-    for (int part = 0; part < 2; ++part) idx[part][ht->pat[part][t]] += ht->code[part][t * N + c];
-  }
-  int best = 0;
-  for (int part = 0; part < 2; ++part) {
-    int s = 0;
-    for (int p = 0; p < NP; ++p) {
-      size_t off = (W == 4) ? ((size_t)p << 20) : (p ? ((size_t)1 << 28) : 0);
-      s += tables[off + idx[part][p]];
-    }
-    best = max(best, s);
-  }
-  hout[i] = best;
+  hout[i] = board_h<W, PDB>(boards + (size_t)i * N, ht, tables);
 }
 
 int grid_for(uint64_t T, int block) {

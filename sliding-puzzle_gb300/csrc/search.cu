@@ -34,8 +34,11 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "../../include/slide.h"
 #include "sp_defs.h"
+#include "sp_device.cuh"
 #include "sp_kernels.h"
 
 namespace sp {
@@ -100,6 +103,14 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
   __shared__ uint32_t s_stack[WORDS][BLOCK];
   __shared__ uint32_t s_prefix[kPathWords][BLOCK];  // the lane's task prefix (its pool slot is freed)
   __shared__ __align__(16) uint8_t s_board[W == 5 ? BLOCK * BSTRIDE : 4];
+  // block-wide cache of the pool state: at most one global poll per block per poll_ns
+  __shared__ uint32_t s_pool[4];  // head, tail, error, outstanding
+  __shared__ unsigned long long s_pool_t;
+  if (threadIdx.x == 0) {
+    s_pool[0] = s_pool[1] = s_pool[2] = 0;
+    s_pool[3] = 1;
+    s_pool_t = 0;
+  }
 
   const HeurTables *ht = P.ht;
   if (PDB) {
@@ -376,9 +387,38 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
 
   unsigned long long last_change = 0;
   uint32_t last_out = 0xFFFFFFFFu, last_tail = 0xFFFFFFFFu;
+  unsigned backoff = 256;  // idle-warp sleep, ns, doubled up to 32 us
+  unsigned long long c_steps = 0, c_slots = 0, c_idle = 0;
+  const long long t_begin = clock64();
 
   for (;;) {
-    // 1. idle lanes claim pool slots, one atomic per warp
+    const long long t_iter = clock64();
+    // 0. pool state from the block's cached copy (one global poll per block
+    //    per poll_ns; a stale copy only delays, never corrupts, decisions:
+    //    outstanding == 0 is final, tail and head only grow)
+    uint32_t hd = 0, tl = 0, out = 0;
+    int32_t err = 0;
+    if (lane == 0) {
+      volatile uint32_t *vp = (volatile uint32_t *)s_pool;
+      const unsigned long long now = globaltimer();
+      if (now - *(volatile unsigned long long *)&s_pool_t > P.poll_ns) {
+        s_pool_t = now;
+        vp[0] = ld_volatile(&ctl->head);
+        vp[1] = ld_volatile(&ctl->tail);
+        vp[2] = (uint32_t)ld_volatile(&ctl->error);
+        vp[3] = ld_volatile(&ctl->outstanding);
+      }
+      hd = vp[0];
+      tl = vp[1];
+      err = (int32_t)vp[2];
+      out = vp[3];
+    }
+    hd = __shfl_sync(FULL, hd, 0);
+    tl = __shfl_sync(FULL, tl, 0);
+    err = __shfl_sync(FULL, err, 0);
+    out = __shfl_sync(FULL, out, 0);
+    if (err) break;
+    // 1. idle lanes claim pool indices, one atomic per warp
     const unsigned need = __ballot_sync(FULL, state == 0);
     if (need) {
       const int leader = __ffs(need) - 1;
@@ -390,8 +430,9 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
         state = 1;
       }
     }
-    // 2. a claimed index becomes a task once its producer published it
-    if (state == 1 && ld_volatile(&P.seq[slot & (P.cap - 1u)]) == slot + 1u) {
+    // 2. a claimed index becomes a task once its producer published it; only
+    //    indices already reserved (below the cached tail) are polled
+    if (state == 1 && slot < tl && ld_volatile(&P.seq[slot & (P.cap - 1u)]) == slot + 1u) {
       __threadfence();
       take_task();
       if (start_task()) state = 2;
@@ -400,12 +441,8 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
     // 3. nobody in the warp is searching: finished, failed or waiting
     const unsigned act = __ballot_sync(FULL, state == 2);
     if (!act) {
-      uint32_t out = 0, tl = 0;
-      int32_t err = 0;
+      if (out == 0) break;
       if (lane == 0) {
-        out = ld_volatile(&ctl->outstanding);
-        tl = ld_volatile(&ctl->tail);
-        err = ld_volatile(&ctl->error);
         const unsigned long long now = globaltimer();
         if (out != last_out || tl != last_tail || last_change == 0) {
           last_out = out;
@@ -413,36 +450,27 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
           last_change = now;
         } else if (now - last_change > P.timeout_ns) {
           set_error(SP_ERR_TIMEOUT, out);
-          err = SP_ERR_TIMEOUT;
         }
       }
-      out = __shfl_sync(FULL, out, 0);
-      err = __shfl_sync(FULL, err, 0);
-      if (out == 0 || err != 0) break;
-      __nanosleep(1000);
+      __nanosleep(backoff);
+      backoff = min(backoff * 2u, 16384u);
+      c_idle += (unsigned long long)(clock64() - t_iter);
       continue;
     }
+    backoff = 256;
+    last_change = 0;  // a new idle spell starts its own no-progress clock
     // 4. search
+    c_slots += 32ull * (unsigned long long)P.steps;
     if (state == 2) {
       for (int s = 0; s < P.steps; ++s) {
+        ++c_steps;
         if (step()) {
           finish_task();
           break;
         }
       }
     }
-    // 5. pool status: errors and hunger
-    uint32_t hd = 0, tl = 0;
-    int32_t err = 0;
-    if (lane == 0) {
-      hd = ld_volatile(&ctl->head);
-      tl = ld_volatile(&ctl->tail);
-      err = ld_volatile(&ctl->error);
-    }
-    hd = __shfl_sync(FULL, hd, 0);
-    tl = __shfl_sync(FULL, tl, 0);
-    err = __shfl_sync(FULL, err, 0);
-    if (err) break;
+    // 5. donate while someone waits (head ahead of tail)
     if (P.donate && hd > tl) {
       uint32_t dmask = 0;
       int lev = (state == 2) ? find_donation(dmask) : -1;
@@ -480,27 +508,131 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
       }
     }
   }
+  // efficiency counters (warp-aggregated)
+  unsigned long long steps_w = c_steps;
+  for (int o = 16; o; o >>= 1) steps_w += __shfl_xor_sync(FULL, steps_w, o);
+  if (lane == 0) {
+    atomicAdd(&ctl->counters[0], steps_w);
+    atomicAdd(&ctl->counters[1], c_slots);
+    atomicAdd(&ctl->counters[2], c_idle);
+    atomicAdd(&ctl->counters[3], (unsigned long long)(clock64() - t_begin));
+  }
 }
 
 // Reset the ring (seq[s] = s: slot s free for index s), fill indices [0, n)
-// with the round's root tasks and publish them (seq = index + 1).
-__global__ void pool_init_kernel(Task *tasks, const Task *init, uint32_t *seq, uint32_t n, uint32_t cap,
-                                 PoolCtl *ctl) {
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) {
-    tasks[i] = init[i];
-    seq[i] = i + 1u;
-  } else if (i < cap) {
-    seq[i] = i;
+// with the round's root tasks and publish them (seq = index + 1).  The pieces
+// of split roots (count on the device) come first, then the host's direct
+// tasks, which the host orders by decreasing predicted size.
+__global__ void pool_init_kernel(Task *tasks, const Task *emit, const uint32_t *n_emit, const Task *direct,
+                                 uint32_t n_direct, uint32_t *seq, uint32_t cap, PoolCtl *ctl) {
+  const uint32_t ne = n_emit ? *n_emit : 0u;
+  const uint32_t n = min(ne + n_direct, cap);
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += gridDim.x * blockDim.x) {
+    if (i < n) {
+      tasks[i] = i < ne ? emit[i] : direct[i - ne];
+      seq[i] = i + 1u;
+    } else {
+      seq[i] = i;
+    }
   }
-  if (i == 0) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
     ctl->head = 0;
     ctl->tail = n;
     ctl->outstanding = n;
-    ctl->error = 0;
+    ctl->error = (ne + n_direct > cap) ? SP_ERR_CAPACITY : 0;
     ctl->donated = 0;
-    ctl->progress_ns = 0;
+    for (int c = 0; c < 8; ++c) ctl->counters[c] = 0;
   }
+}
+
+// One breadth-first level of the split pre-pass: each input node (a root, or
+// a piece of one, at f <= limit) is expanded; every legal non-reverse child
+// is counted as generated, exactly as the depth-first search would count it,
+// and children within the limit go on to the next level or, at the last
+// level, become pool tasks.  flags = levels still to expand.
+template <int W, bool PDB>
+__global__ void split_level_kernel(SplitArgs A) {
+  constexpr int N = W * W;
+  const uint32_t n_in = *A.n_in;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n_in; i += gridDim.x * blockDim.x) {
+    const Task T = A.in[i];
+    const SubRoot R = A.subs[T.sub];
+    uint8_t b[N];
+    for (int c = 0; c < N; ++c) b[c] = R.board[c];
+    int blank = R.blank, g = R.g, pre = R.pre == kNoPre ? -1 : (int)R.pre;
+    bool ok = true;
+    for (int q = 0; q < T.plen; ++q) {
+      const int d = (int)((T.path[q >> 4] >> (2 * (q & 15))) & 3u);
+      if (!((legal_moves(W, blank) >> d) & 1u)) { ok = false; break; }
+      const int src = blank + move_delta(W, d);
+      b[blank] = b[src];
+      b[src] = 0;
+      blank = src;
+      pre = d;
+      ++g;
+    }
+    if (!ok) {
+      atomicCAS(A.error, 0, SP_ERR_ARG);
+      continue;
+    }
+    const int L = A.inst_limit[R.inst];
+    uint32_t mv = legal_moves(W, blank) & T.mask;
+    if (pre >= 0) mv &= ~(1u << (3 - pre));
+    unsigned long long cnt = 0;
+    for (int d = 0; d < 4; ++d) {
+      if (!((mv >> d) & 1u)) continue;
+      ++cnt;
+      const int src = blank + move_delta(W, d);
+      b[blank] = b[src];
+      b[src] = 0;
+      const int hc = board_h<W, PDB>(b, A.ht, A.pdb);
+      b[src] = b[blank];
+      b[blank] = 0;
+      if (g + 1 + hc > L) continue;
+      Task C = T;
+      const int q = T.plen;
+      if (q >= kMaxPath) {
+        atomicCAS(A.error, 0, SP_ERR_STACK_OVERFLOW);
+        continue;
+      }
+      C.path[q >> 4] = (C.path[q >> 4] & ~(3u << (2 * (q & 15)))) | ((uint32_t)d << (2 * (q & 15)));
+      C.plen = (uint16_t)(q + 1);
+      C.mask = 0xF;
+      C.flags = (uint8_t)(T.flags - 1);
+      if (hc == 0) {  // a goal at the child: record it like the search does
+        Solution *S = &A.sol[R.inst];
+        if (atomicCAS(&S->flag, 0u, 1u) == 0u) {
+          S->sub = T.sub;
+          S->len = (uint32_t)(q + 1);
+          for (int wi = 0; wi < kPathWords; ++wi) S->path[wi] = C.path[wi];
+          __threadfence();
+        }
+      }
+      if (C.flags > 0) {
+        const uint32_t at = atomicAdd(A.n_next, 1u);
+        if (at < A.cap_next) A.next[at] = C;
+        else atomicCAS(A.error, 0, SP_ERR_CAPACITY);
+      } else {
+        const uint32_t at = atomicAdd(A.n_out, 1u);
+        if (at < A.cap_out) A.out[at] = C;
+        else atomicCAS(A.error, 0, SP_ERR_CAPACITY);
+      }
+    }
+    if (cnt) atomicAdd(&A.sub_nodes[T.sub], cnt);
+  }
+}
+
+cudaError_t launch_split_level(int w, bool pdb, int num_sms, const SplitArgs &A, cudaStream_t st) {
+  const int grid = num_sms * 8, block = 128;
+  if (w == 4) {
+    if (pdb) split_level_kernel<4, true><<<grid, block, 0, st>>>(A);
+    else split_level_kernel<4, false><<<grid, block, 0, st>>>(A);
+  } else {
+    if (pdb) split_level_kernel<5, true><<<grid, block, 0, st>>>(A);
+    else split_level_kernel<5, false><<<grid, block, 0, st>>>(A);
+  }
+  note_launch();
+  return cudaGetLastError();
 }
 
 // Host launchers (template kernels stay in this translation unit).
@@ -532,10 +664,10 @@ cudaError_t launch_search_round(int w, bool pdb, int block, int blocks_per_sm, i
   return cudaGetLastError();
 }
 
-cudaError_t launch_pool_init(Task *tasks, const Task *init, uint32_t *seq, uint32_t n, uint32_t cap,
-                             PoolCtl *ctl, cudaStream_t st) {
-  const uint32_t blocks = (cap + 255) / 256;
-  pool_init_kernel<<<blocks, 256, 0, st>>>(tasks, init, seq, n, cap, ctl);
+cudaError_t launch_pool_init(Task *tasks, const Task *emit, const uint32_t *n_emit, const Task *direct,
+                             uint32_t n_direct, uint32_t *seq, uint32_t cap, PoolCtl *ctl, cudaStream_t st) {
+  const uint32_t blocks = std::min<uint32_t>((cap + 255) / 256, 152u * 32u);
+  pool_init_kernel<<<blocks, 256, 0, st>>>(tasks, emit, n_emit, direct, n_direct, seq, cap, ctl);
   note_launch();
   return cudaGetLastError();
 }

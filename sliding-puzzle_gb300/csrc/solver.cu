@@ -65,6 +65,8 @@ struct Instance {
   std::vector<TreeNode> tree;
   std::vector<int32_t> leaves;      // tree indices of root-set members
   std::vector<uint64_t> last_load;  // per leaf, previous round
+  uint64_t last_total = 0;          // device nodes of the previous round
+  uint64_t prev_total = 0;          // and of the one before
   sp_result *out = nullptr;
 };
 
@@ -108,7 +110,12 @@ struct sp_solver {
   bool pdb_ready = false;
   uint32_t import_mask = 0;
   double pdb_build_ms = 0;
-  int last_grid = 0;
+  int last_lanes = 0;       // lanes of the last search launch
+  uint32_t last_emitted = 0;
+  // split pre-pass buffers
+  uint32_t *d_cnt = nullptr;  // [level a, level b, emitted, error]
+  Task *d_split_a = nullptr, *d_split_b = nullptr, *d_emit = nullptr;
+  size_t split_cap_a = 0, split_cap_b = 0, emit_cap = 0;
   // device task pool
   Task *d_tasks = nullptr;
   uint32_t *d_seq = nullptr;
@@ -277,22 +284,6 @@ int compute_tree_h(sp_solver *s, std::vector<Instance> &inst, const std::vector<
   return SP_OK;
 }
 
-// Expand leaf `leaf` of an instance's tree breadth-first until it has at
-// least `pieces` leaves below it (or the depth budget runs out).
-void split_leaf(int w, Instance &I, int leaf, int pieces, int max_extra_depth) {
-  std::vector<int32_t> level{leaf};
-  for (int dep = 0; dep < max_extra_depth && (int)level.size() < pieces; ++dep) {
-    std::vector<int32_t> next;
-    for (int32_t x : level) {
-      size_t before = I.tree.size();
-      expand_node(w, I.tree, x);
-      for (size_t c = before; c < I.tree.size(); ++c) next.push_back((int32_t)c);
-    }
-    if (next.empty()) break;
-    level.swap(next);
-  }
-}
-
 void rebuild_leaves(Instance &I) {
   I.leaves.clear();
   for (size_t j = 0; j < I.tree.size(); ++j)
@@ -320,36 +311,6 @@ bool replay_ok(int w, const uint8_t *tiles, const uint8_t *moves, int len) {
   return true;
 }
 
-int launch_round(sp_solver *s, uint32_t n_init, float *ms) {
-  SP_CUDA(s, launch_pool_init(s->d_tasks, s->d_init, s->d_seq, n_init, s->cap, s->d_ctl, s->st));
-  RoundParams P{};
-  P.subs = s->d_subs;
-  P.tasks = s->d_tasks;
-  P.seq = s->d_seq;
-  P.cap = s->cap;
-  P.ctl = s->d_ctl;
-  P.inst_limit = s->d_limit;
-  P.sub_nodes = s->d_sub_nodes;
-  P.sol = s->d_sol;
-  P.ht = s->d_ht;
-  P.pdb = s->d_pdb;
-  P.min_slack = s->cfg.donate_min_slack;
-  P.steps = s->cfg.steps_per_poll;
-  P.donate = s->cfg.lb_mode == SP_LB_NONE ? 0 : 1;
-  P.timeout_ns = (unsigned long long)s->cfg.timeout_ms * 1000000ull;
-  const int block = s->cfg.threads_per_block == 128 ? 128 : 256;
-  SP_CUDA(s, cudaEventRecord(s->ev0, s->st));
-  int grid = 0;
-  SP_CUDA(s, launch_search_round(s->w, s->heur == SP_HEUR_PDB, block, s->cfg.blocks_per_sm, s->num_sms, P,
-                                 s->st, &grid));
-  SP_CUDA(s, cudaEventRecord(s->ev1, s->st));
-  SP_CUDA(s, cudaEventSynchronize(s->ev1));
-  SP_CUDA(s, cudaEventElapsedTime(ms, s->ev0, s->ev1));
-  s->stats.kernel_launches += 2;
-  s->last_grid = grid;
-  return SP_OK;
-}
-
 // Ring capacity: a power of two holding the round's root tasks plus room for
 // a waiting claim from every resident lane.
 int ensure_pool(sp_solver *s, size_t n_init) {
@@ -369,6 +330,176 @@ int ensure_pool(sp_solver *s, size_t n_init) {
   SP_CUDA(s, cudaMalloc(&s->d_seq, need * sizeof(uint32_t)));
   s->cap = (uint32_t)need;
   return SP_OK;
+}
+
+// The round's work: tasks started as they are, and roots expanded `flags`
+// levels by the device split pre-pass first.
+struct RoundPlan {
+  std::vector<Task> direct;
+  std::vector<Task> split;
+  size_t level_bound = 0;  // nodes one split level can hold
+  size_t emit_bound = 0;   // pieces the split pre-pass can emit
+  int max_k = 0;
+};
+
+int launch_round(sp_solver *s, const RoundPlan &plan, float *ms, uint32_t *split_err) {
+  const uint32_t n_direct = (uint32_t)plan.direct.size();
+  int rc = ensure_pool(s, plan.direct.size() + plan.emit_bound);
+  if (rc) return rc;
+  rc = ensure(s, &s->d_init, &s->init_cap, std::max<size_t>(plan.direct.size(), 1));
+  if (rc) return rc;
+  if (!s->d_cnt) SP_CUDA(s, cudaMalloc(&s->d_cnt, 4 * sizeof(uint32_t)));
+  if (n_direct) {
+    SP_CUDA(s, cudaMemcpyAsync(s->d_init, plan.direct.data(), n_direct * sizeof(Task), cudaMemcpyHostToDevice, s->st));
+    s->stats.h2d_bytes += n_direct * sizeof(Task);
+  }
+  uint32_t cnt0[4] = {(uint32_t)plan.split.size(), 0, 0, 0};
+  SP_CUDA(s, cudaMemcpyAsync(s->d_cnt, cnt0, sizeof(cnt0), cudaMemcpyHostToDevice, s->st));
+  if (!plan.split.empty()) {
+    rc = ensure(s, &s->d_split_a, &s->split_cap_a, std::max(plan.level_bound, plan.split.size()));
+    if (rc) return rc;
+    rc = ensure(s, &s->d_split_b, &s->split_cap_b, std::max(plan.level_bound, plan.split.size()));
+    if (rc) return rc;
+    rc = ensure(s, &s->d_emit, &s->emit_cap, std::max<size_t>(plan.emit_bound, 1));
+    if (rc) return rc;
+    SP_CUDA(s, cudaMemcpyAsync(s->d_split_a, plan.split.data(), plan.split.size() * sizeof(Task),
+                               cudaMemcpyHostToDevice, s->st));
+    s->stats.h2d_bytes += plan.split.size() * sizeof(Task);
+  }
+  SP_CUDA(s, cudaEventRecord(s->ev0, s->st));
+  for (int l = 0; l < plan.max_k; ++l) {
+    const int cur = l & 1, nxt = cur ^ 1;
+    SP_CUDA(s, cudaMemsetAsync(s->d_cnt + nxt, 0, sizeof(uint32_t), s->st));
+    SplitArgs A{};
+    A.subs = s->d_subs;
+    A.inst_limit = s->d_limit;
+    A.ht = s->d_ht;
+    A.pdb = s->d_pdb;
+    A.sub_nodes = s->d_sub_nodes;
+    A.sol = s->d_sol;
+    A.in = cur ? s->d_split_b : s->d_split_a;
+    A.n_in = s->d_cnt + cur;
+    A.next = nxt ? s->d_split_b : s->d_split_a;
+    A.n_next = s->d_cnt + nxt;
+    A.cap_next = (uint32_t)(nxt ? s->split_cap_b : s->split_cap_a);
+    A.out = s->d_emit;
+    A.n_out = s->d_cnt + 2;
+    A.cap_out = (uint32_t)s->emit_cap;
+    A.error = (int32_t *)(s->d_cnt + 3);
+    SP_CUDA(s, launch_split_level(s->w, s->heur == SP_HEUR_PDB, s->num_sms, A, s->st));
+    s->stats.kernel_launches += 1;
+  }
+  SP_CUDA(s, launch_pool_init(s->d_tasks, s->d_emit, plan.max_k ? s->d_cnt + 2 : nullptr, s->d_init, n_direct,
+                              s->d_seq, s->cap, s->d_ctl, s->st));
+  RoundParams P{};
+  P.subs = s->d_subs;
+  P.tasks = s->d_tasks;
+  P.seq = s->d_seq;
+  P.cap = s->cap;
+  P.ctl = s->d_ctl;
+  P.inst_limit = s->d_limit;
+  P.sub_nodes = s->d_sub_nodes;
+  P.sol = s->d_sol;
+  P.ht = s->d_ht;
+  P.pdb = s->d_pdb;
+  P.min_slack = s->cfg.donate_min_slack;
+  P.steps = s->cfg.steps_per_poll;
+  P.donate = s->cfg.lb_mode == SP_LB_NONE ? 0 : 1;
+  P.timeout_ns = (unsigned long long)s->cfg.timeout_ms * 1000000ull;
+  P.poll_ns = 2000;
+  const int block = s->cfg.threads_per_block == 128 ? 128 : 256;
+  SP_CUDA(s, cudaEventRecord(s->ev0, s->st));
+  int grid = 0;
+  SP_CUDA(s, launch_search_round(s->w, s->heur == SP_HEUR_PDB, block, s->cfg.blocks_per_sm, s->num_sms, P,
+                                 s->st, &grid));
+  SP_CUDA(s, cudaEventRecord(s->ev1, s->st));
+  uint32_t cnt[4] = {0, 0, 0, 0};
+  SP_CUDA(s, cudaMemcpyAsync(cnt, s->d_cnt, sizeof(cnt), cudaMemcpyDeviceToHost, s->st));
+  SP_CUDA(s, cudaEventSynchronize(s->ev1));
+  SP_CUDA(s, cudaStreamSynchronize(s->st));
+  SP_CUDA(s, cudaEventElapsedTime(ms, s->ev0, s->ev1));
+  *split_err = cnt[3];
+  s->stats.kernel_launches += 2;
+  s->last_lanes = grid * block;
+  s->last_emitted = cnt[2];
+  return SP_OK;
+}
+
+// Static load balancing for the next round: a root's work is predicted from
+// its previous round (load x the instance's growth per threshold step); a
+// root predicted above the round's piece size T is split ceil(log2(pred/T))
+// levels by the device pre-pass -- the reference splits a root into
+// ceil(load/avg) pieces (src/24puzzle_block_parallel_with_pdb.cu:839-897) --
+// and direct tasks are published in decreasing predicted size.
+void plan_static(sp_solver *s, std::vector<Instance> &inst, const std::vector<int32_t> &limits,
+                 RoundPlan &plan) {
+  struct Cand {
+    double pred;
+    Task t;
+    int room;  // levels left below the root before the limit
+  };
+  std::vector<Cand> c;
+  double total = 0;
+  for (size_t i = 0; i < inst.size(); ++i) {
+    Instance &I = inst[i];
+    if (I.done) continue;
+    double growth = 6.0;
+    if (I.prev_total > 0 && I.last_total > 0) growth = std::min(30.0, std::max(2.0, (double)I.last_total / I.prev_total));
+    for (size_t q = 0; q < I.leaves.size(); ++q) {
+      const TreeNode &t = I.tree[(size_t)I.leaves[q]];
+      if (t.maxf > limits[i]) continue;
+      Cand x;
+      x.pred = (double)I.last_load[q] * growth;
+      x.t = Task{};
+      x.t.sub = (uint32_t)t.sub;
+      x.t.mask = 0xF;
+      x.room = limits[i] - t.g;
+      total += x.pred;
+      c.push_back(x);
+    }
+  }
+  const double lanes = s->last_lanes > 0 ? (double)s->last_lanes : (double)s->num_sms * 1024.0;
+  const double T = total / (lanes * 4.0);
+  size_t budget = (size_t)1 << 22;
+  plan.max_k = 0;
+  std::vector<int> k(c.size(), 0);
+  if (T > 0 && s->cfg.lb_mode == SP_LB_STATIC_STEAL) {
+    for (size_t j = 0; j < c.size(); ++j) {
+      if (c[j].pred > T) {
+        int kk = (int)std::ceil(std::log2(c[j].pred / T));
+        kk = std::min(kk, std::min(10, std::max(0, c[j].room - 1)));
+        k[j] = std::max(0, std::min(kk, std::max(1, s->cfg.static_split_cap)));
+      }
+    }
+    auto bound = [&](int kk) { return kk ? (size_t)4 * (size_t)std::pow(3.0, kk - 1) : 0; };
+    size_t need = 0;
+    for (int kk : k) need += bound(kk);
+    while (need > budget) {  // trim the deepest splits first
+      int mk = 0;
+      for (int kk : k) mk = std::max(mk, kk);
+      if (!mk) break;
+      for (auto &kk : k)
+        if (kk == mk) { need -= bound(kk) - bound(kk - 1); --kk; }
+    }
+  }
+  std::vector<size_t> order(c.size());
+  for (size_t j = 0; j < c.size(); ++j) order[j] = j;
+  if (s->cfg.lb_mode == SP_LB_STATIC_STEAL)
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return c[a].pred > c[b].pred; });
+  std::vector<size_t> level(12, 0);
+  for (size_t j : order) {
+    if (k[j] > 0) {
+      Task t = c[j].t;
+      t.flags = (uint8_t)k[j];
+      plan.split.push_back(t);
+      plan.max_k = std::max(plan.max_k, k[j]);
+      for (int l = 1; l <= k[j]; ++l) level[(size_t)l] += (size_t)4 * (size_t)std::pow(3.0, l - 1);
+      plan.emit_bound += (size_t)4 * (size_t)std::pow(3.0, k[j] - 1);
+    } else {
+      plan.direct.push_back(c[j].t);
+    }
+  }
+  for (size_t l = 1; l < level.size(); ++l) plan.level_bound = std::max(plan.level_bound, level[l]);
 }
 
 int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
@@ -431,9 +562,12 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
   bool subs_dirty = true;
 
   for (int round = 0; round < SP_MAX_ITERS; ++round) {
-    bool any = false;
-    for (auto &I : inst) any |= !I.done;
-    if (!any) break;
+    int active = 0;
+    for (auto &I : inst) active += !I.done;
+    if (!active) break;
+    const auto t_round = std::chrono::steady_clock::now();
+    const int ri = std::min(round, SP_MAX_ROUNDS - 1);
+    s->stats.round_instances[ri] = active;
     // (re)build the SubRoot array when the trees changed
     if (subs_dirty) {
       subs.clear();
@@ -466,7 +600,6 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
       subs_dirty = false;
     }
     // per instance: interior counts, host-side goals, active roots
-    init.clear();
     std::vector<uint64_t> interior(inst.size(), 0);
     std::vector<int32_t> host_goal(inst.size(), -1);
     for (size_t i = 0; i < inst.size(); ++i) {
@@ -480,21 +613,10 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
         if (t.h == 0 && (host_goal[i] < 0 || t.g < I.tree[(size_t)host_goal[i]].g)) host_goal[i] = (int32_t)j;
         if (!t.leaf) interior[i] += t.nchild;
       }
-      for (int32_t x : I.leaves) {
-        const TreeNode &t = I.tree[(size_t)x];
-        if (t.maxf > L) continue;
-        Task tk{};
-        tk.sub = (uint32_t)t.sub;
-        tk.plen = 0;
-        tk.mask = 0xF;
-        init.push_back(tk);
-      }
     }
-    // launch
-    rc = ensure_pool(s, init.size());
-    if (rc) return rc;
-    rc = ensure(s, &s->d_init, &s->init_cap, std::max<size_t>(init.size(), 1));
-    if (rc) return rc;
+    RoundPlan plan;
+    plan_static(s, inst, limits, plan);
+    const size_t n_tasks = plan.direct.size() + plan.split.size();
     if (inst.size() > s->inst_cap || !s->d_limit) {
       if (s->d_limit) cudaFree(s->d_limit);
       if (s->d_sol) cudaFree(s->d_sol);
@@ -505,20 +627,17 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
       SP_CUDA(s, cudaMalloc(&s->d_sol, c * sizeof(Solution)));
       s->inst_cap = c;
     }
-    if (!init.empty()) {
-      SP_CUDA(s, cudaMemcpyAsync(s->d_init, init.data(), init.size() * sizeof(Task), cudaMemcpyHostToDevice, s->st));
-      s->stats.h2d_bytes += init.size() * sizeof(Task);
-    }
     SP_CUDA(s, cudaMemcpyAsync(s->d_limit, limits.data(), inst.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s->st));
     SP_CUDA(s, cudaMemsetAsync(s->d_sol, 0, inst.size() * sizeof(Solution), s->st));
     SP_CUDA(s, cudaMemsetAsync(s->d_sub_nodes, 0, std::max<size_t>(subs.size(), 1) * sizeof(unsigned long long), s->st));
     s->stats.h2d_bytes += inst.size() * sizeof(int32_t);
     float ms = 0;
-    if (!init.empty()) {
-      rc = launch_round(s, (uint32_t)init.size(), &ms);
+    if (n_tasks) {
+      uint32_t split_err = 0;
+      rc = launch_round(s, plan, &ms, &split_err);
       if (rc) return rc;
       s->stats.kernel_ms += ms;
-      s->stats.tasks_initial += init.size();
+      s->stats.tasks_initial += plan.direct.size() + s->last_emitted;
       PoolCtl ctl{};
       SP_CUDA(s, cudaMemcpyAsync(&ctl, s->d_ctl, sizeof(PoolCtl), cudaMemcpyDeviceToHost, s->st));
       sub_nodes.assign(subs.size(), 0);
@@ -528,6 +647,14 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
       SP_CUDA(s, cudaStreamSynchronize(s->st));
       s->stats.d2h_bytes += sizeof(PoolCtl) + subs.size() * 8 + inst.size() * sizeof(Solution);
       s->stats.tasks_donated += ctl.donated;
+      s->stats.dev_lane_steps += ctl.counters[0];
+      s->stats.dev_lane_slots += ctl.counters[1];
+      s->stats.dev_idle_cycles += ctl.counters[2];
+      s->stats.dev_warp_cycles += ctl.counters[3];
+      s->stats.round_tasks[ri] = (int32_t)(plan.direct.size() + s->last_emitted);
+      s->stats.round_kernel_ms[ri] = ms;
+      s->stats.round_donated[ri] = ctl.donated;
+      if (!ctl.error && split_err) ctl.error = (int32_t)split_err;
       if (ctl.error) {
         char buf[160];
         snprintf(buf, sizeof buf, "device error %d (info %u) in round %d", ctl.error, ctl.err_info[0], round);
@@ -545,18 +672,22 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
     for (size_t i = 0; i < inst.size(); ++i) {
       Instance &I = inst[i];
       if (I.done) continue;
-      uint64_t nodes = interior[i];
+      uint64_t nodes = interior[i], dev = 0;
       for (size_t q = 0; q < I.leaves.size(); ++q) {
         const uint64_t v = sub_nodes[(size_t)I.tree[(size_t)I.leaves[q]].sub];
-        nodes += v;
+        dev += v;
         I.last_load[q] = v;
       }
+      nodes += dev;
+      I.prev_total = I.last_total;
+      I.last_total = dev;
       sp_result *R = I.out;
       R->f_limit[I.iter] = limits[i];
       R->nodes[I.iter] = nodes;
       R->nodes_total += nodes;
       R->n_iter = I.iter + 1;
       s->stats.nodes += nodes;
+      s->stats.round_nodes[ri] += nodes;
       const bool dev_goal = sols[i].flag != 0;
       if (host_goal[i] >= 0 || dev_goal) {
         // path: root-set tree prefix, then the device's moves below its root
@@ -591,36 +722,7 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
         I.done = true;
       }
     }
-    // static load balancing: split heavy roots for the next round
-    if (s->cfg.lb_mode == SP_LB_STATIC_STEAL) {
-      std::vector<size_t> before(inst.size());
-      bool changed = false;
-      for (size_t i = 0; i < inst.size(); ++i) {
-        Instance &I = inst[i];
-        before[i] = I.tree.size();
-        if (I.done || I.leaves.empty()) continue;
-        uint64_t sum = 0;
-        for (uint64_t v : I.last_load) sum += v;
-        const uint64_t avg = sum / I.leaves.size();
-        if (!avg) continue;
-        const size_t cap_leaves = 65536;
-        for (size_t q = 0; q < I.leaves.size() && I.tree.size() < cap_leaves * 2; ++q) {
-          const uint64_t ld = I.last_load[q];
-          int pieces = (int)std::min<uint64_t>((ld - 1) / avg + 1, (uint64_t)std::max(2, s->cfg.static_split_cap));
-          if (ld > avg && pieces > 1) {
-            split_leaf(w, I, I.leaves[q], pieces, 8);
-            changed = true;
-          }
-        }
-      }
-      if (changed) {
-        rc = compute_tree_h(s, inst, before);
-        if (rc) return rc;
-        for (auto &I : inst)
-          if (!I.done) rebuild_leaves(I);
-        subs_dirty = true;
-      }
-    }
+    s->stats.round_host_ms[ri] = (float)(ms_since(t_round) - s->stats.round_kernel_ms[ri]);
   }
   const double wall = ms_since(t_start);
   for (auto &I : inst) {
@@ -706,6 +808,10 @@ void sp_destroy(sp_solver *s) {
   cudaFree(s->d_sol);
   cudaFree(s->d_boards);
   cudaFree(s->d_h);
+  cudaFree(s->d_cnt);
+  cudaFree(s->d_split_a);
+  cudaFree(s->d_split_b);
+  cudaFree(s->d_emit);
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->st) cudaStreamDestroy(s->st);
@@ -850,10 +956,6 @@ int sp_dfs_round(sp_solver *s, const uint8_t *roots, const int32_t *depth, const
     if (h[(size_t)i] == 0 && (*found < 0 || depth[i] < *found)) *found = depth[i];
   rc = ensure(s, &s->d_subs, &s->subs_cap, (size_t)n);
   if (rc) return rc;
-  rc = ensure(s, &s->d_init, &s->init_cap, (size_t)n);
-  if (rc) return rc;
-  rc = ensure_pool(s, (size_t)n);
-  if (rc) return rc;
   if (!s->d_limit || s->inst_cap < 1) {
     SP_CUDA(s, cudaMalloc(&s->d_limit, 64 * sizeof(int32_t)));
     SP_CUDA(s, cudaMalloc(&s->d_sol, 64 * sizeof(Solution)));
@@ -863,12 +965,14 @@ int sp_dfs_round(sp_solver *s, const uint8_t *roots, const int32_t *depth, const
   s->d_sub_nodes = nullptr;
   SP_CUDA(s, cudaMalloc(&s->d_sub_nodes, (size_t)n * sizeof(unsigned long long)));
   SP_CUDA(s, cudaMemcpyAsync(s->d_subs, subs.data(), subs.size() * sizeof(SubRoot), cudaMemcpyHostToDevice, s->st));
-  SP_CUDA(s, cudaMemcpyAsync(s->d_init, init.data(), init.size() * sizeof(Task), cudaMemcpyHostToDevice, s->st));
   SP_CUDA(s, cudaMemcpyAsync(s->d_limit, &limit, sizeof(int32_t), cudaMemcpyHostToDevice, s->st));
   SP_CUDA(s, cudaMemsetAsync(s->d_sol, 0, sizeof(Solution), s->st));
   SP_CUDA(s, cudaMemsetAsync(s->d_sub_nodes, 0, (size_t)n * sizeof(unsigned long long), s->st));
   float ms = 0;
-  rc = launch_round(s, (uint32_t)n, &ms);
+  RoundPlan plan;
+  plan.direct = std::move(init);
+  uint32_t split_err = 0;
+  rc = launch_round(s, plan, &ms, &split_err);
   if (rc) return rc;
   PoolCtl ctl{};
   Solution sol{};
@@ -878,6 +982,15 @@ int sp_dfs_round(sp_solver *s, const uint8_t *roots, const int32_t *depth, const
   SP_CUDA(s, cudaStreamSynchronize(s->st));
   s->stats.kernel_ms = ms;
   s->stats.rounds = 1;
+  s->stats.tasks_initial = (uint64_t)n;
+  s->stats.tasks_donated = ctl.donated;
+  s->stats.dev_lane_steps = ctl.counters[0];
+  s->stats.dev_lane_slots = ctl.counters[1];
+  s->stats.dev_idle_cycles = ctl.counters[2];
+  s->stats.dev_warp_cycles = ctl.counters[3];
+  s->stats.round_tasks[0] = n;
+  s->stats.round_kernel_ms[0] = ms;
+  s->stats.round_donated[0] = ctl.donated;
   if (ctl.error) {
     s->err = "device error in sp_dfs_round";
     return ctl.error;

@@ -113,16 +113,28 @@ struct Solution {
 };
 static_assert(sizeof(Solution) == 64, "Solution layout");
 
-// Pool control block (one per round, zeroed/initialised by the host).
+// Pool control block (reset by pool_init_kernel each round).  Each hot word
+// has its own 128-byte line so claims, publications, completions and error
+// polls do not queue behind each other in one L2 slice.
 struct PoolCtl {
-  uint32_t head;          // next slot to claim (may run ahead of tail)
-  uint32_t tail;          // slots reserved by producers
+  uint32_t head;          // next index to claim (may run ahead of tail)
+  uint32_t pad0[31];
+  uint32_t tail;          // indices reserved by producers
+  uint32_t pad1[31];
   uint32_t outstanding;   // tasks queued or running
+  uint32_t pad2[31];
   int32_t error;          // first device error (sp_status)
-  unsigned long long donated;
-  unsigned long long progress_ns;
   uint32_t err_info[4];
+  uint32_t pad3[27];
+  unsigned long long donated;
+  unsigned long long pad4[15];
+  // efficiency counters, one atomic per warp at exit:
+  // [0] step() calls (active lane-steps)  [1] warp step iterations x 32
+  // [2] clock cycles warps spent with no active lane  [3] total warp cycles
+  unsigned long long counters[8];
+  unsigned long long pad5[8];
 };
+static_assert(sizeof(PoolCtl) == 768, "PoolCtl layout");
 
 // Heuristic lookup tables built once per solver.
 struct HeurTables {

@@ -27,14 +27,35 @@ struct RoundParams {
   int32_t donate;
   int32_t pad;
   unsigned long long timeout_ns;
+  unsigned long long poll_ns;  // min interval of a block's global pool poll
 };
 
 // One threshold round: grid = num_sms * blocks_per_sm (0 = occupancy maximum).
 cudaError_t launch_search_round(int w, bool pdb, int block, int blocks_per_sm, int num_sms,
                                 const RoundParams &P, cudaStream_t st, int *grid_out);
-// Publish the round's first n tasks and reset the pool control block.
-cudaError_t launch_pool_init(Task *tasks, const Task *init, uint32_t *seq, uint32_t n, uint32_t cap,
-                             PoolCtl *ctl, cudaStream_t st);
+// Publish the round's tasks (split pieces first, then the direct tasks) and
+// reset the pool control block.
+cudaError_t launch_pool_init(Task *tasks, const Task *emit, const uint32_t *n_emit, const Task *direct,
+                             uint32_t n_direct, uint32_t *seq, uint32_t cap, PoolCtl *ctl, cudaStream_t st);
+
+// Split pre-pass: one breadth-first level over `in` (count *n_in).
+struct SplitArgs {
+  const SubRoot *subs;
+  const int32_t *inst_limit;
+  const HeurTables *ht;
+  const uint8_t *pdb;
+  unsigned long long *sub_nodes;
+  Solution *sol;
+  const Task *in;
+  const uint32_t *n_in;
+  Task *next;
+  uint32_t *n_next;
+  Task *out;
+  uint32_t *n_out;
+  uint32_t cap_next, cap_out;
+  int32_t *error;
+};
+cudaError_t launch_split_level(int w, bool pdb, int num_sms, const SplitArgs &A, cudaStream_t st);
 
 // h of n boards (n * N bytes) into h[n]; PDB tables as in RoundParams.
 cudaError_t launch_heuristic(int w, bool pdb, const uint8_t *boards, int n, int32_t *h,

@@ -42,11 +42,20 @@ class SpResult(ctypes.Structure):
                 ("moves", ctypes.c_uint8 * SP_MAX_MOVES), ("seconds", ctypes.c_double)]
 
 
+SP_MAX_ROUNDS = 96
+
+
 class SpStats(ctypes.Structure):
     _fields_ = [("frontier_ms", ctypes.c_double), ("kernel_ms", ctypes.c_double), ("wall_ms", ctypes.c_double),
                 ("rounds", ctypes.c_int32), ("kernel_launches", ctypes.c_int32),
                 ("tasks_initial", ctypes.c_uint64), ("tasks_donated", ctypes.c_uint64),
-                ("nodes", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64)]
+                ("nodes", ctypes.c_uint64), ("h2d_bytes", ctypes.c_uint64), ("d2h_bytes", ctypes.c_uint64),
+                ("round_instances", ctypes.c_int32 * SP_MAX_ROUNDS), ("round_tasks", ctypes.c_int32 * SP_MAX_ROUNDS),
+                ("round_kernel_ms", ctypes.c_float * SP_MAX_ROUNDS),
+                ("round_host_ms", ctypes.c_float * SP_MAX_ROUNDS),
+                ("round_nodes", ctypes.c_uint64 * SP_MAX_ROUNDS), ("round_donated", ctypes.c_uint64 * SP_MAX_ROUNDS),
+                ("dev_lane_steps", ctypes.c_uint64), ("dev_lane_slots", ctypes.c_uint64),
+                ("dev_idle_cycles", ctypes.c_uint64), ("dev_warp_cycles", ctypes.c_uint64)]
 
 
 _lib = None
@@ -217,7 +226,11 @@ class Solver:
     def stats(self):
         s = SpStats()
         self._check(self.lib.sp_last_stats(self.h, ctypes.byref(s)), "sp_last_stats")
-        return {f: getattr(s, f) for f, _ in SpStats._fields_}
+        out = {}
+        for f, _ in SpStats._fields_:
+            v = getattr(s, f)
+            out[f] = list(v)[: s.rounds] if f.startswith("round_") else v
+        return out
 
 
 def result_dict(r):
