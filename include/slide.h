@@ -116,6 +116,10 @@ typedef struct {
   uint64_t dev_lane_slots;   /* lane slots offered by warps' step loops */
   uint64_t dev_idle_cycles;  /* warp cycles with no lane searching */
   uint64_t dev_warp_cycles;  /* all warp cycles */
+  uint64_t dev_donate_tries;    /* donation attempts by a warp's chosen lane */
+  uint64_t dev_donate_notfree;  /* ... refused: the ring slot still occupied */
+  uint64_t dev_donate_nowait;   /* ... refused: no lane waiting any more */
+  uint64_t dev_tasks_done;      /* tasks finished */
 } sp_stats;
 
 typedef struct sp_solver sp_solver;

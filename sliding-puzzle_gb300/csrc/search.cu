@@ -45,11 +45,26 @@ namespace sp {
 
 namespace {
 
+// Pool words are read with GPU-scope relaxed loads (coherent across SMs, never
+// served from a stale L1 line); readiness of a slot with an acquire load, so
+// the record written before its release store is visible.
 __device__ __forceinline__ uint32_t ld_volatile(const uint32_t *p) {
-  return *(const volatile uint32_t *)p;
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
 }
 __device__ __forceinline__ int32_t ld_volatile(const int32_t *p) {
-  return *(const volatile int32_t *)p;
+  int32_t v;
+  asm volatile("ld.relaxed.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
+  uint32_t v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 __device__ __forceinline__ unsigned long long globaltimer() {
   unsigned long long t;
@@ -145,6 +160,7 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
   uint32_t hvr = 0, hvf = 0;
   ir.clear();
   iff.clear();
+  unsigned long long c_tries = 0, c_notfree = 0, c_nowait = 0, c_done = 0;  // donation counters
 
   auto tile_at = [&](int c) -> int {
     if (W == 4) return (int)((b64 >> (4 * c)) & 15u);
@@ -213,6 +229,7 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
     if (atomicCAS(&ctl->error, 0, code) == 0) ctl->err_info[0] = info;
   };
   auto finish_task = [&]() {
+    ++c_done;
     if (cnt) atomicAdd(&P.sub_nodes[sub], cnt);
     __threadfence();
     atomicSub(&ctl->outstanding, 1u);
@@ -228,8 +245,7 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
     plen = (int)(hdr & 0xFFFFu);
     mask0 = (hdr >> 16) & 0xFu;
     for (int wi = 0; wi < kPathWords; ++wi) s_prefix[wi][tid] = __ldcg(&T->path[wi]);
-    __threadfence();
-    atomicExch(&P.seq[s], slot + P.cap);
+    st_release(&P.seq[s], slot + P.cap);  // the copy above completes before the slot is reused
   };
   auto start_task = [&]() -> bool {
     const SubRoot *R = &P.subs[sub];
@@ -432,8 +448,7 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
     }
     // 2. a claimed index becomes a task once its producer published it; only
     //    indices already reserved (below the cached tail) are polled
-    if (state == 1 && slot < tl && ld_volatile(&P.seq[slot & (P.cap - 1u)]) == slot + 1u) {
-      __threadfence();
+    if (state == 1 && slot < tl && ld_acquire(&P.seq[slot & (P.cap - 1u)]) == slot + 1u) {
       take_task();
       if (start_task()) state = 2;
       else finish_task();
@@ -479,17 +494,22 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
       const unsigned key = lev >= 0 ? ((unsigned)lev << 5) | (unsigned)lane : 0xFFFFFFFFu;
       const unsigned best = __reduce_min_sync(FULL, key);
       if (best != 0xFFFFFFFFu && (int)(best & 31u) == lane) {
-        // reserve index t only while someone waits for it (t < head) and its
-        // ring slot is free (its previous occupant, t - cap, was taken)
+        // reserve the next index; its ring slot is free once the slot's previous
+        // occupant (index t - cap, claimed long before) was copied out, which
+        // in practice it already is -- wait a bounded time, else leave the
+        // index unpublished (its claimant then idles until the round ends)
         const uint32_t mask = P.cap - 1u;
-        uint32_t t = ld_volatile(&ctl->tail), hh = ld_volatile(&ctl->head);
+        ++c_tries;
+        const uint32_t t = atomicAdd(&ctl->tail, 1u);
         bool ok = false;
-        while (t < hh && ld_volatile(&P.seq[t & mask]) == t) {
-          const uint32_t old = atomicCAS(&ctl->tail, t, t + 1);
-          if (old == t) { ok = true; break; }
-          t = old;
-          hh = ld_volatile(&ctl->head);
+        for (int spin = 0; spin < 4096; ++spin) {
+          if (ld_acquire(&P.seq[t & mask]) == t) {
+            ok = true;
+            break;
+          }
+          __nanosleep(64);
         }
+        if (!ok) ++c_notfree;
         if (ok) {
           atomicAdd(&ctl->outstanding, 1u);
           Task *D = &P.tasks[t & mask];
@@ -499,8 +519,7 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
           D->mask = (uint8_t)dmask;
           D->flags = 1;
           for (int wi = 0; wi < kPathWords; ++wi) D->path[wi] = path_word(wi, nlen);
-          __threadfence();
-          atomicExch(&P.seq[t & mask], t + 1u);
+          st_release(&P.seq[t & mask], t + 1u);
           atomicAdd(&ctl->donated, 1ull);
           if (lev == k) it = 4;
           else cut |= 1ull << lev;
@@ -509,13 +528,24 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
     }
   }
   // efficiency counters (warp-aggregated)
-  unsigned long long steps_w = c_steps;
-  for (int o = 16; o; o >>= 1) steps_w += __shfl_xor_sync(FULL, steps_w, o);
+  unsigned long long steps_w = c_steps, tries_w = c_tries, notfree_w = c_notfree, nowait_w = c_nowait,
+                     done_w = c_done;
+  for (int o = 16; o; o >>= 1) {
+    steps_w += __shfl_xor_sync(FULL, steps_w, o);
+    tries_w += __shfl_xor_sync(FULL, tries_w, o);
+    notfree_w += __shfl_xor_sync(FULL, notfree_w, o);
+    nowait_w += __shfl_xor_sync(FULL, nowait_w, o);
+    done_w += __shfl_xor_sync(FULL, done_w, o);
+  }
   if (lane == 0) {
     atomicAdd(&ctl->counters[0], steps_w);
     atomicAdd(&ctl->counters[1], c_slots);
     atomicAdd(&ctl->counters[2], c_idle);
     atomicAdd(&ctl->counters[3], (unsigned long long)(clock64() - t_begin));
+    atomicAdd(&ctl->counters[4], tries_w);
+    atomicAdd(&ctl->counters[5], notfree_w);
+    atomicAdd(&ctl->counters[6], nowait_w);
+    atomicAdd(&ctl->counters[7], done_w);
   }
 }
 

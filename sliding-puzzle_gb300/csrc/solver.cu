@@ -651,6 +651,10 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
       s->stats.dev_lane_slots += ctl.counters[1];
       s->stats.dev_idle_cycles += ctl.counters[2];
       s->stats.dev_warp_cycles += ctl.counters[3];
+      s->stats.dev_donate_tries += ctl.counters[4];
+      s->stats.dev_donate_notfree += ctl.counters[5];
+      s->stats.dev_donate_nowait += ctl.counters[6];
+      s->stats.dev_tasks_done += ctl.counters[7];
       s->stats.round_tasks[ri] = (int32_t)(plan.direct.size() + s->last_emitted);
       s->stats.round_kernel_ms[ri] = ms;
       s->stats.round_donated[ri] = ctl.donated;
@@ -988,11 +992,21 @@ int sp_dfs_round(sp_solver *s, const uint8_t *roots, const int32_t *depth, const
   s->stats.dev_lane_slots = ctl.counters[1];
   s->stats.dev_idle_cycles = ctl.counters[2];
   s->stats.dev_warp_cycles = ctl.counters[3];
+  s->stats.dev_donate_tries = ctl.counters[4];
+  s->stats.dev_donate_notfree = ctl.counters[5];
+  s->stats.dev_donate_nowait = ctl.counters[6];
+  s->stats.dev_tasks_done = ctl.counters[7];
   s->stats.round_tasks[0] = n;
   s->stats.round_kernel_ms[0] = ms;
   s->stats.round_donated[0] = ctl.donated;
   if (ctl.error) {
-    s->err = "device error in sp_dfs_round";
+    char buf[320];
+    snprintf(buf, sizeof buf,
+             "device error %d (info %u) in sp_dfs_round: donated %llu tries %llu notfree %llu nowait %llu done %llu",
+             ctl.error, ctl.err_info[0], (unsigned long long)ctl.donated, (unsigned long long)ctl.counters[4],
+             (unsigned long long)ctl.counters[5], (unsigned long long)ctl.counters[6],
+             (unsigned long long)ctl.counters[7]);
+    s->err = buf;
     return ctl.error;
   }
   if (sol.flag) {

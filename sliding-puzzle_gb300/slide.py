@@ -55,7 +55,9 @@ class SpStats(ctypes.Structure):
                 ("round_host_ms", ctypes.c_float * SP_MAX_ROUNDS),
                 ("round_nodes", ctypes.c_uint64 * SP_MAX_ROUNDS), ("round_donated", ctypes.c_uint64 * SP_MAX_ROUNDS),
                 ("dev_lane_steps", ctypes.c_uint64), ("dev_lane_slots", ctypes.c_uint64),
-                ("dev_idle_cycles", ctypes.c_uint64), ("dev_warp_cycles", ctypes.c_uint64)]
+                ("dev_idle_cycles", ctypes.c_uint64), ("dev_warp_cycles", ctypes.c_uint64),
+                ("dev_donate_tries", ctypes.c_uint64), ("dev_donate_notfree", ctypes.c_uint64),
+                ("dev_donate_nowait", ctypes.c_uint64), ("dev_tasks_done", ctypes.c_uint64)]
 
 
 _lib = None
