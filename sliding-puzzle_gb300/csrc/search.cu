@@ -119,10 +119,10 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
   __shared__ uint32_t s_prefix[kPathWords][BLOCK];  // the lane's task prefix (its pool slot is freed)
   __shared__ __align__(16) uint8_t s_board[W == 5 ? BLOCK * BSTRIDE : 4];
   // block-wide cache of the pool state: at most one global poll per block per poll_ns
-  __shared__ uint32_t s_pool[4];  // head, tail, error, outstanding
+  __shared__ uint32_t s_pool[5];  // head, tail, error, outstanding, heartbeat
   __shared__ unsigned long long s_pool_t;
   if (threadIdx.x == 0) {
-    s_pool[0] = s_pool[1] = s_pool[2] = 0;
+    s_pool[0] = s_pool[1] = s_pool[2] = s_pool[4] = 0;
     s_pool[3] = 1;
     s_pool_t = 0;
   }
@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
   uint32_t hvr = 0, hvf = 0;
   ir.clear();
   iff.clear();
-  unsigned long long c_tries = 0, c_notfree = 0, c_nowait = 0, c_done = 0;  // donation counters
+  unsigned long long c_tries = 0, c_notfree = 0, c_nowait = 0, c_done = 0, c_found = 0;  // donation counters
 
   auto tile_at = [&](int c) -> int {
     if (W == 4) return (int)((b64 >> (4 * c)) & 15u);
@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
   };
 
   unsigned long long last_change = 0;
-  uint32_t last_out = 0xFFFFFFFFu, last_tail = 0xFFFFFFFFu;
+  uint32_t last_out = 0xFFFFFFFFu, last_tail = 0xFFFFFFFFu, last_hb = 0xFFFFFFFFu, beat = 0;
   unsigned backoff = 256;  // idle-warp sleep, ns, doubled up to 32 us
   unsigned long long c_steps = 0, c_slots = 0, c_idle = 0;
   const long long t_begin = clock64();
@@ -412,7 +412,7 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
     // 0. pool state from the block's cached copy (one global poll per block
     //    per poll_ns; a stale copy only delays, never corrupts, decisions:
     //    outstanding == 0 is final, tail and head only grow)
-    uint32_t hd = 0, tl = 0, out = 0;
+    uint32_t hd = 0, tl = 0, out = 0, hb = 0;
     int32_t err = 0;
     if (lane == 0) {
       volatile uint32_t *vp = (volatile uint32_t *)s_pool;
@@ -423,11 +423,13 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
         vp[1] = ld_volatile(&ctl->tail);
         vp[2] = (uint32_t)ld_volatile(&ctl->error);
         vp[3] = ld_volatile(&ctl->outstanding);
+        vp[4] = ld_volatile(&ctl->heartbeat);
       }
       hd = vp[0];
       tl = vp[1];
       err = (int32_t)vp[2];
       out = vp[3];
+      hb = vp[4];
     }
     hd = __shfl_sync(FULL, hd, 0);
     tl = __shfl_sync(FULL, tl, 0);
@@ -459,9 +461,10 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
       if (out == 0) break;
       if (lane == 0) {
         const unsigned long long now = globaltimer();
-        if (out != last_out || tl != last_tail || last_change == 0) {
+        if (out != last_out || tl != last_tail || hb != last_hb || last_change == 0) {
           last_out = out;
           last_tail = tl;
+          last_hb = hb;
           last_change = now;
         } else if (now - last_change > P.timeout_ns) {
           set_error(SP_ERR_TIMEOUT, out);
@@ -474,6 +477,7 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
     }
     backoff = 256;
     last_change = 0;  // a new idle spell starts its own no-progress clock
+    if (lane == 0 && ((++beat & 127u) == 0u)) atomicAdd(&ctl->heartbeat, 1u);
     // 4. search
     c_slots += 32ull * (unsigned long long)P.steps;
     if (state == 2) {
@@ -493,6 +497,10 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
       // one donor per warp per poll: the lane with the shallowest level
       const unsigned key = lev >= 0 ? ((unsigned)lev << 5) | (unsigned)lane : 0xFFFFFFFFu;
       const unsigned best = __reduce_min_sync(FULL, key);
+      if (lane == 0) {
+        ++c_nowait;  // hungry polls
+        if (best != 0xFFFFFFFFu) ++c_found;
+      }
       if (best != 0xFFFFFFFFu && (int)(best & 31u) == lane) {
         // reserve the next index; its ring slot is free once the slot's previous
         // occupant (index t - cap, claimed long before) was copied out, which
@@ -546,6 +554,7 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
     atomicAdd(&ctl->counters[5], notfree_w);
     atomicAdd(&ctl->counters[6], nowait_w);
     atomicAdd(&ctl->counters[7], done_w);
+    atomicAdd(&ctl->counters[8], c_found);
   }
 }
 
@@ -571,7 +580,8 @@ __global__ void pool_init_kernel(Task *tasks, const Task *emit, const uint32_t *
     ctl->outstanding = n;
     ctl->error = (ne + n_direct > cap) ? SP_ERR_CAPACITY : 0;
     ctl->donated = 0;
-    for (int c = 0; c < 8; ++c) ctl->counters[c] = 0;
+    ctl->heartbeat = 0;
+    for (int c = 0; c < 16; ++c) ctl->counters[c] = 0;
   }
 }
 

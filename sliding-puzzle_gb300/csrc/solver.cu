@@ -1002,10 +1002,11 @@ int sp_dfs_round(sp_solver *s, const uint8_t *roots, const int32_t *depth, const
   if (ctl.error) {
     char buf[320];
     snprintf(buf, sizeof buf,
-             "device error %d (info %u) in sp_dfs_round: donated %llu tries %llu notfree %llu nowait %llu done %llu",
+             "device error %d (info %u) in sp_dfs_round: donated %llu tries %llu notfree %llu hungry-polls %llu "
+             "donor-found %llu done %llu",
              ctl.error, ctl.err_info[0], (unsigned long long)ctl.donated, (unsigned long long)ctl.counters[4],
              (unsigned long long)ctl.counters[5], (unsigned long long)ctl.counters[6],
-             (unsigned long long)ctl.counters[7]);
+             (unsigned long long)ctl.counters[8], (unsigned long long)ctl.counters[7]);
     s->err = buf;
     return ctl.error;
   }

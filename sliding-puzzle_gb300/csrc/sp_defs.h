@@ -128,13 +128,15 @@ struct PoolCtl {
   uint32_t pad3[27];
   unsigned long long donated;
   unsigned long long pad4[15];
+  uint32_t heartbeat;     // bumped by searching warps: a long task is progress too
+  uint32_t pad6[31];
   // efficiency counters, one atomic per warp at exit:
   // [0] step() calls (active lane-steps)  [1] warp step iterations x 32
   // [2] clock cycles warps spent with no active lane  [3] total warp cycles
-  unsigned long long counters[8];
-  unsigned long long pad5[8];
+  unsigned long long counters[16];  // [4] donation tries [5] slot never freed [6] hungry
+                                    // polls [7] tasks done [8] polls with a donor found
 };
-static_assert(sizeof(PoolCtl) == 768, "PoolCtl layout");
+static_assert(sizeof(PoolCtl) == 896, "PoolCtl layout");
 
 // Heuristic lookup tables built once per solver.
 struct HeurTables {
