@@ -562,13 +562,20 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
 // with the round's root tasks and publish them (seq = index + 1).  The pieces
 // of split roots (count on the device) come first, then the host's direct
 // tasks, which the host orders by decreasing predicted size.
-__global__ void pool_init_kernel(Task *tasks, const Task *emit, const uint32_t *n_emit, const Task *direct,
+__global__ void pool_init_kernel(Task *tasks, const Task *emit, const uint32_t *n_emit, const uint32_t *direct,
                                  uint32_t n_direct, uint32_t *seq, uint32_t cap, PoolCtl *ctl) {
   const uint32_t ne = n_emit ? *n_emit : 0u;
   const uint32_t n = min(ne + n_direct, cap);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += gridDim.x * blockDim.x) {
     if (i < n) {
-      tasks[i] = i < ne ? emit[i] : direct[i - ne];
+      if (i < ne) {
+        tasks[i] = emit[i];
+      } else {  // a whole root: no prefix, every first move
+        Task t{};
+        t.sub = direct[i - ne];
+        t.mask = 0xF;
+        tasks[i] = t;
+      }
       seq[i] = i + 1u;
     } else {
       seq[i] = i;
@@ -704,7 +711,7 @@ cudaError_t launch_search_round(int w, bool pdb, int block, int blocks_per_sm, i
   return cudaGetLastError();
 }
 
-cudaError_t launch_pool_init(Task *tasks, const Task *emit, const uint32_t *n_emit, const Task *direct,
+cudaError_t launch_pool_init(Task *tasks, const Task *emit, const uint32_t *n_emit, const uint32_t *direct,
                              uint32_t n_direct, uint32_t *seq, uint32_t cap, PoolCtl *ctl, cudaStream_t st) {
   const uint32_t blocks = std::min<uint32_t>((cap + 255) / 256, 152u * 32u);
   pool_init_kernel<<<blocks, 256, 0, st>>>(tasks, emit, n_emit, direct, n_direct, seq, cap, ctl);

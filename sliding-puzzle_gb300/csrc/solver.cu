@@ -5,7 +5,7 @@
 // Reference counterparts:
 //   create_root_set       src/24puzzle_block_parallel_with_pdb.cu:454-490
 //   ida_star round loop   src/24puzzle_block_parallel_with_pdb.cu:756-922
-//   divide_root_set       src/24puzzle_block_parallel_with_pdb.cu:652-747
+//   static re-split       src/24puzzle_block_parallel_with_pdb.cu:839-897
 //
 // Differences that keep node counts exact (the reference's GPU solvers
 // report lengths only):
@@ -18,9 +18,8 @@
 //     whose path stays within the limit (prefix maximum of g+h: the PDB
 //     heuristic is not consistent, so f can drop along a path), and a root
 //     becomes a device task only if the same holds for it;
-//   * the static re-split of heavy roots (ceil(load/avg) pieces, as at
-//     :839-897) refines the root-set tree, so the pieces' ancestors are
-//     counted like any other interior node.
+//   * heavy roots are split by the device pre-pass (search.cu), which counts
+//     the nodes it expands like the search would.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -28,6 +27,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <memory>
 #include <string>
@@ -52,9 +52,7 @@ struct TreeNode {
   int32_t maxf;                 // max of g+h over the path root..this node
   uint8_t nchild;               // legal non-reverse children
   uint8_t leaf;                 // 1: root-set member (device task when active)
-  uint8_t expanded;             // children present in the tree
-  uint8_t pad;
-  int32_t sub;                  // index into the batch's SubRoot array, -1 if none
+  uint8_t pad[2];
 };
 
 struct Instance {
@@ -63,10 +61,15 @@ struct Instance {
   int iter = 0;
   bool done = false;
   std::vector<TreeNode> tree;
-  std::vector<int32_t> leaves;      // tree indices of root-set members
-  std::vector<uint64_t> last_load;  // per leaf, previous round
-  uint64_t last_total = 0;          // device nodes of the previous round
-  uint64_t prev_total = 0;          // and of the one before
+  // after h is known: root-set leaves sorted by maxf (the active leaves of a
+  // round are a prefix), interior nodes as (maxf, cumulative children)
+  std::vector<int32_t> leaves;
+  std::vector<int32_t> leaf_maxf;
+  std::vector<std::pair<int32_t, uint64_t>> interior;
+  std::vector<int32_t> goals;        // tree nodes with h == 0
+  std::vector<uint64_t> last_load;   // per leaf, previous round
+  uint64_t last_total = 0, prev_total = 0;
+  uint32_t sub_base = 0;             // SubRoot index of leaves[0]
   sp_result *out = nullptr;
 };
 
@@ -92,6 +95,26 @@ int check_instance(int w, const uint8_t *t) {
   const int par = (w & 1) ? (inv & 1) : ((inv + brow) & 1);
   return par ? SP_ERR_UNSOLVABLE : SP_OK;
 }
+
+// Grow-only pinned host buffer.
+template <typename T>
+struct Pinned {
+  T *p = nullptr;
+  size_t cap = 0;
+  ~Pinned() {
+    if (p) cudaFreeHost(p);
+  }
+  cudaError_t reserve(size_t n) {
+    if (n <= cap && p) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    size_t c = std::max<size_t>(n, 1024);
+    cudaError_t e = cudaMallocHost((void **)&p, c * sizeof(T));
+    if (e == cudaSuccess) cap = c;
+    return e;
+  }
+};
 
 }  // namespace
 }  // namespace sp
@@ -121,20 +144,26 @@ struct sp_solver {
   uint32_t *d_seq = nullptr;
   uint32_t cap = 0;
   PoolCtl *d_ctl = nullptr;
-  uint32_t stamp = 0;
   // per-batch buffers
   SubRoot *d_subs = nullptr;
   size_t subs_cap = 0;
-  Task *d_init = nullptr;
-  size_t init_cap = 0;
+  uint32_t *d_direct = nullptr;
+  size_t direct_cap = 0;
   unsigned long long *d_sub_nodes = nullptr;
+  size_t sub_nodes_cap = 0;
   int32_t *d_limit = nullptr;
   Solution *d_sol = nullptr;
   size_t inst_cap = 0;
   uint8_t *d_boards = nullptr;
   int32_t *d_h = nullptr;
-  size_t boards_cap = 0;
-  size_t h_cap = 0;
+  size_t boards_cap = 0, h_cap = 0;
+  // pinned staging
+  Pinned<uint32_t> h_direct;
+  Pinned<unsigned long long> h_sub_nodes;
+  Pinned<Solution> h_sols;
+  Pinned<PoolCtl> h_ctl;
+  Pinned<int32_t> h_limits;
+  Pinned<uint32_t> h_cnt;
   std::string err;
   sp_stats stats{};
 };
@@ -207,19 +236,17 @@ void make_root(int w, const uint8_t *tiles, TreeNode *r) {
     r->board[i] = tiles[i];
     if (!tiles[i]) r->blank = (uint8_t)i;
   }
-  r->g = 0;
   r->pre = kNoPre;
   r->move = kNoPre;
   r->parent = -1;
-  r->sub = -1;
+  r->leaf = 1;
 }
 
-// Append the children of tree[idx]; returns how many.
-int expand_node(int w, std::vector<TreeNode> &tree, int idx) {
-  TreeNode p = tree[idx];
+// Append the children of tree[idx] (legal, not reversing its move).
+void expand_node(int w, std::vector<TreeNode> &tree, int idx) {
+  const TreeNode p = tree[(size_t)idx];
   uint32_t mv = legal_moves(w, p.blank);
   if (p.pre != kNoPre) mv &= ~(1u << (3 - p.pre));
-  int cnt = 0;
   for (int d = 0; d < 4; ++d) {
     if (!((mv >> d) & 1u)) continue;
     TreeNode c = p;
@@ -231,17 +258,10 @@ int expand_node(int w, std::vector<TreeNode> &tree, int idx) {
     c.pre = (uint8_t)d;
     c.move = (uint8_t)d;
     c.parent = idx;
-    c.h = 0;
-    c.maxf = 0;
     c.leaf = 1;
-    c.expanded = 0;
-    c.sub = -1;
     tree.push_back(c);
-    ++cnt;
   }
-  tree[idx].expanded = 1;
-  tree[idx].leaf = 0;
-  return cnt;
+  tree[(size_t)idx].leaf = 0;
 }
 
 uint8_t count_children(int w, const TreeNode &t) {
@@ -250,45 +270,74 @@ uint8_t count_children(int w, const TreeNode &t) {
   return (uint8_t)__builtin_popcount(mv);
 }
 
-// h for tree nodes [from, tree.size()) of every instance, on the GPU.
-int compute_tree_h(sp_solver *s, std::vector<Instance> &inst, const std::vector<size_t> &from) {
+// h of every tree node of every instance, on the GPU; then maxf, children,
+// the leaves sorted by maxf and the interior prefix sums.
+int finish_trees(sp_solver *s, std::vector<Instance> &inst) {
   size_t total = 0;
-  for (size_t i = 0; i < inst.size(); ++i) total += inst[i].tree.size() - from[i];
+  for (auto &I : inst) total += I.tree.size();
   if (!total) return SP_OK;
   int rc = ensure(s, &s->d_boards, &s->boards_cap, total * (size_t)s->n);
   if (rc) return rc;
   rc = ensure(s, &s->d_h, &s->h_cap, total);
   if (rc) return rc;
-  std::vector<uint8_t> boards(total * (size_t)s->n);
+  Pinned<uint8_t> boards;
+  Pinned<int32_t> hv;
+  SP_CUDA(s, boards.reserve(total * (size_t)s->n));
+  SP_CUDA(s, hv.reserve(total));
   size_t o = 0;
-  for (size_t i = 0; i < inst.size(); ++i)
-    for (size_t j = from[i]; j < inst[i].tree.size(); ++j, ++o)
-      memcpy(&boards[o * s->n], inst[i].tree[j].board, (size_t)s->n);
-  SP_CUDA(s, cudaMemcpyAsync(s->d_boards, boards.data(), boards.size(), cudaMemcpyHostToDevice, s->st));
-  s->stats.h2d_bytes += boards.size();
+  for (auto &I : inst)
+    for (auto &t : I.tree) memcpy(boards.p + (o++) * s->n, t.board, (size_t)s->n);
+  SP_CUDA(s, cudaMemcpyAsync(s->d_boards, boards.p, total * s->n, cudaMemcpyHostToDevice, s->st));
+  s->stats.h2d_bytes += total * s->n;
   SP_CUDA(s, launch_heuristic(s->w, s->heur == SP_HEUR_PDB, s->d_boards, (int)total, s->d_h, s->d_ht,
                               s->d_pdb, s->st));
-  std::vector<int32_t> hv(total);
-  SP_CUDA(s, cudaMemcpyAsync(hv.data(), s->d_h, total * sizeof(int32_t), cudaMemcpyDeviceToHost, s->st));
+  SP_CUDA(s, cudaMemcpyAsync(hv.p, s->d_h, total * sizeof(int32_t), cudaMemcpyDeviceToHost, s->st));
   SP_CUDA(s, cudaStreamSynchronize(s->st));
   s->stats.d2h_bytes += total * sizeof(int32_t);
   o = 0;
-  for (size_t i = 0; i < inst.size(); ++i)
-    for (size_t j = from[i]; j < inst[i].tree.size(); ++j, ++o) {
-      TreeNode &t = inst[i].tree[j];
-      t.h = hv[o];
+  for (auto &I : inst) {
+    for (auto &t : I.tree) {
+      t.h = hv.p[o++];
       const int f = (int)t.g + t.h;
-      t.maxf = t.parent < 0 ? f : std::max(inst[i].tree[t.parent].maxf, f);
+      t.maxf = t.parent < 0 ? f : std::max(I.tree[(size_t)t.parent].maxf, f);
       t.nchild = count_children(s->w, t);
     }
+    if (I.done) continue;
+    I.h0 = I.tree[0].h;
+    I.leaves.clear();
+    std::vector<std::pair<int32_t, uint8_t>> interior;
+    for (size_t j = 0; j < I.tree.size(); ++j) {
+      const TreeNode &t = I.tree[j];
+      if (t.leaf) I.leaves.push_back((int32_t)j);
+      else interior.push_back({t.maxf, t.nchild});
+      if (t.h == 0) I.goals.push_back((int32_t)j);
+    }
+    std::stable_sort(I.leaves.begin(), I.leaves.end(),
+                     [&](int32_t a, int32_t b) { return I.tree[(size_t)a].maxf < I.tree[(size_t)b].maxf; });
+    I.leaf_maxf.resize(I.leaves.size());
+    for (size_t q = 0; q < I.leaves.size(); ++q) I.leaf_maxf[q] = I.tree[(size_t)I.leaves[q]].maxf;
+    std::sort(interior.begin(), interior.end());
+    I.interior.clear();
+    uint64_t cum = 0;
+    for (auto &x : interior) {
+      cum += x.second;
+      if (!I.interior.empty() && I.interior.back().first == x.first) I.interior.back().second = cum;
+      else I.interior.push_back({x.first, cum});
+    }
+    I.last_load.assign(I.leaves.size(), 0);
+  }
   return SP_OK;
 }
 
-void rebuild_leaves(Instance &I) {
-  I.leaves.clear();
-  for (size_t j = 0; j < I.tree.size(); ++j)
-    if (I.tree[j].leaf) I.leaves.push_back((int32_t)j);
-  I.last_load.assign(I.leaves.size(), 0);
+// children generated this round by interior nodes within the limit
+uint64_t interior_nodes(const Instance &I, int L) {
+  auto it = std::upper_bound(I.interior.begin(), I.interior.end(), L,
+                             [](int32_t v, const std::pair<int32_t, uint64_t> &e) { return v < e.first; });
+  return it == I.interior.begin() ? 0 : std::prev(it)->second;
+}
+
+size_t active_leaves(const Instance &I, int L) {
+  return (size_t)(std::upper_bound(I.leaf_maxf.begin(), I.leaf_maxf.end(), L) - I.leaf_maxf.begin());
 }
 
 bool replay_ok(int w, const uint8_t *tiles, const uint8_t *moves, int len) {
@@ -332,33 +381,58 @@ int ensure_pool(sp_solver *s, size_t n_init) {
   return SP_OK;
 }
 
-// The round's work: tasks started as they are, and roots expanded `flags`
-// levels by the device split pre-pass first.
+// The round's work: whole roots started as they are (direct, SubRoot ids in
+// publication order) and roots first expanded `flags` levels by the split
+// pre-pass.
 struct RoundPlan {
-  std::vector<Task> direct;
+  std::vector<uint32_t> direct;
   std::vector<Task> split;
   size_t level_bound = 0;  // nodes one split level can hold
   size_t emit_bound = 0;   // pieces the split pre-pass can emit
   int max_k = 0;
 };
 
-int launch_round(sp_solver *s, const RoundPlan &plan, float *ms, uint32_t *split_err) {
+void fold_ctl(sp_solver *s, const PoolCtl &ctl, int ri, float ms) {
+  sp_stats &x = s->stats;
+  x.kernel_ms += ms;
+  x.tasks_donated += ctl.donated;
+  x.dev_lane_steps += ctl.counters[0];
+  x.dev_lane_slots += ctl.counters[1];
+  x.dev_idle_cycles += ctl.counters[2];
+  x.dev_warp_cycles += ctl.counters[3];
+  x.dev_donate_tries += ctl.counters[4];
+  x.dev_donate_notfree += ctl.counters[5];
+  x.dev_donate_nowait += ctl.counters[6];
+  x.dev_tasks_done += ctl.counters[7];
+  x.round_kernel_ms[ri] = ms;
+  x.round_donated[ri] = ctl.donated;
+}
+
+// Launch one round: uploads, split pre-pass, pool set-up, search; then the
+// control block, split counters, per-root counts and solutions come back.
+int launch_round(sp_solver *s, const RoundPlan &plan, size_t n_subs, size_t n_inst, float *ms) {
   const uint32_t n_direct = (uint32_t)plan.direct.size();
   int rc = ensure_pool(s, plan.direct.size() + plan.emit_bound);
   if (rc) return rc;
-  rc = ensure(s, &s->d_init, &s->init_cap, std::max<size_t>(plan.direct.size(), 1));
+  rc = ensure(s, &s->d_direct, &s->direct_cap, std::max<size_t>(n_direct, 1));
   if (rc) return rc;
   if (!s->d_cnt) SP_CUDA(s, cudaMalloc(&s->d_cnt, 4 * sizeof(uint32_t)));
+  SP_CUDA(s, s->h_cnt.reserve(4));
   if (n_direct) {
-    SP_CUDA(s, cudaMemcpyAsync(s->d_init, plan.direct.data(), n_direct * sizeof(Task), cudaMemcpyHostToDevice, s->st));
-    s->stats.h2d_bytes += n_direct * sizeof(Task);
+    SP_CUDA(s, s->h_direct.reserve(n_direct));
+    memcpy(s->h_direct.p, plan.direct.data(), n_direct * sizeof(uint32_t));
+    SP_CUDA(s, cudaMemcpyAsync(s->d_direct, s->h_direct.p, n_direct * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                               s->st));
+    s->stats.h2d_bytes += n_direct * sizeof(uint32_t);
   }
-  uint32_t cnt0[4] = {(uint32_t)plan.split.size(), 0, 0, 0};
-  SP_CUDA(s, cudaMemcpyAsync(s->d_cnt, cnt0, sizeof(cnt0), cudaMemcpyHostToDevice, s->st));
+  s->h_cnt.p[0] = (uint32_t)plan.split.size();
+  s->h_cnt.p[1] = s->h_cnt.p[2] = s->h_cnt.p[3] = 0;
+  SP_CUDA(s, cudaMemcpyAsync(s->d_cnt, s->h_cnt.p, 4 * sizeof(uint32_t), cudaMemcpyHostToDevice, s->st));
   if (!plan.split.empty()) {
-    rc = ensure(s, &s->d_split_a, &s->split_cap_a, std::max(plan.level_bound, plan.split.size()));
+    const size_t lb = std::max(plan.level_bound, plan.split.size());
+    rc = ensure(s, &s->d_split_a, &s->split_cap_a, lb);
     if (rc) return rc;
-    rc = ensure(s, &s->d_split_b, &s->split_cap_b, std::max(plan.level_bound, plan.split.size()));
+    rc = ensure(s, &s->d_split_b, &s->split_cap_b, lb);
     if (rc) return rc;
     rc = ensure(s, &s->d_emit, &s->emit_cap, std::max<size_t>(plan.emit_bound, 1));
     if (rc) return rc;
@@ -389,7 +463,7 @@ int launch_round(sp_solver *s, const RoundPlan &plan, float *ms, uint32_t *split
     SP_CUDA(s, launch_split_level(s->w, s->heur == SP_HEUR_PDB, s->num_sms, A, s->st));
     s->stats.kernel_launches += 1;
   }
-  SP_CUDA(s, launch_pool_init(s->d_tasks, s->d_emit, plan.max_k ? s->d_cnt + 2 : nullptr, s->d_init, n_direct,
+  SP_CUDA(s, launch_pool_init(s->d_tasks, s->d_emit, plan.max_k ? s->d_cnt + 2 : nullptr, s->d_direct, n_direct,
                               s->d_seq, s->cap, s->d_ctl, s->st));
   RoundParams P{};
   P.subs = s->d_subs;
@@ -408,34 +482,42 @@ int launch_round(sp_solver *s, const RoundPlan &plan, float *ms, uint32_t *split
   P.timeout_ns = (unsigned long long)s->cfg.timeout_ms * 1000000ull;
   P.poll_ns = 2000;
   const int block = s->cfg.threads_per_block == 128 ? 128 : 256;
-  SP_CUDA(s, cudaEventRecord(s->ev0, s->st));
   int grid = 0;
   SP_CUDA(s, launch_search_round(s->w, s->heur == SP_HEUR_PDB, block, s->cfg.blocks_per_sm, s->num_sms, P,
                                  s->st, &grid));
   SP_CUDA(s, cudaEventRecord(s->ev1, s->st));
-  uint32_t cnt[4] = {0, 0, 0, 0};
-  SP_CUDA(s, cudaMemcpyAsync(cnt, s->d_cnt, sizeof(cnt), cudaMemcpyDeviceToHost, s->st));
-  SP_CUDA(s, cudaEventSynchronize(s->ev1));
+  SP_CUDA(s, s->h_ctl.reserve(1));
+  SP_CUDA(s, s->h_sub_nodes.reserve(std::max<size_t>(n_subs, 1)));
+  SP_CUDA(s, s->h_sols.reserve(std::max<size_t>(n_inst, 1)));
+  SP_CUDA(s, cudaMemcpyAsync(s->h_ctl.p, s->d_ctl, sizeof(PoolCtl), cudaMemcpyDeviceToHost, s->st));
+  SP_CUDA(s, cudaMemcpyAsync(s->h_cnt.p, s->d_cnt, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s->st));
+  if (n_subs)
+    SP_CUDA(s, cudaMemcpyAsync(s->h_sub_nodes.p, s->d_sub_nodes, n_subs * sizeof(unsigned long long),
+                               cudaMemcpyDeviceToHost, s->st));
+  if (n_inst)
+    SP_CUDA(s, cudaMemcpyAsync(s->h_sols.p, s->d_sol, n_inst * sizeof(Solution), cudaMemcpyDeviceToHost, s->st));
   SP_CUDA(s, cudaStreamSynchronize(s->st));
   SP_CUDA(s, cudaEventElapsedTime(ms, s->ev0, s->ev1));
-  *split_err = cnt[3];
+  s->stats.d2h_bytes += sizeof(PoolCtl) + 16 + n_subs * 8 + n_inst * sizeof(Solution);
   s->stats.kernel_launches += 2;
   s->last_lanes = grid * block;
-  s->last_emitted = cnt[2];
+  s->last_emitted = s->h_cnt.p[2];
+  if (!s->h_ctl.p->error && s->h_cnt.p[3]) s->h_ctl.p->error = (int32_t)s->h_cnt.p[3];
   return SP_OK;
 }
 
-// Static load balancing for the next round: a root's work is predicted from
-// its previous round (load x the instance's growth per threshold step); a
-// root predicted above the round's piece size T is split ceil(log2(pred/T))
+// Static load balancing for the round: a root's work is predicted from its
+// previous round (load x the instance's growth per threshold step); a root
+// predicted above the round's piece size T is split ceil(log2(pred/T))
 // levels by the device pre-pass -- the reference splits a root into
 // ceil(load/avg) pieces (src/24puzzle_block_parallel_with_pdb.cu:839-897) --
-// and direct tasks are published in decreasing predicted size.
-void plan_static(sp_solver *s, std::vector<Instance> &inst, const std::vector<int32_t> &limits,
-                 RoundPlan &plan) {
+// and whole roots are published in decreasing predicted size.
+void plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int32_t> &limits,
+                RoundPlan &plan) {
+  const bool stat = s->cfg.lb_mode == SP_LB_STATIC_STEAL;
   struct Cand {
     double pred;
-    Task t;
+    uint32_t sub;
     int room;  // levels left below the root before the limit
   };
   std::vector<Cand> c;
@@ -443,63 +525,65 @@ void plan_static(sp_solver *s, std::vector<Instance> &inst, const std::vector<in
   for (size_t i = 0; i < inst.size(); ++i) {
     Instance &I = inst[i];
     if (I.done) continue;
+    const size_t na = active_leaves(I, limits[i]);
+    if (!stat) {
+      for (size_t q = 0; q < na; ++q) plan.direct.push_back(I.sub_base + (uint32_t)q);
+      continue;
+    }
     double growth = 6.0;
-    if (I.prev_total > 0 && I.last_total > 0) growth = std::min(30.0, std::max(2.0, (double)I.last_total / I.prev_total));
-    for (size_t q = 0; q < I.leaves.size(); ++q) {
-      const TreeNode &t = I.tree[(size_t)I.leaves[q]];
-      if (t.maxf > limits[i]) continue;
-      Cand x;
-      x.pred = (double)I.last_load[q] * growth;
-      x.t = Task{};
-      x.t.sub = (uint32_t)t.sub;
-      x.t.mask = 0xF;
-      x.room = limits[i] - t.g;
-      total += x.pred;
-      c.push_back(x);
+    if (I.prev_total > 0 && I.last_total > 0)
+      growth = std::min(30.0, std::max(2.0, (double)I.last_total / (double)I.prev_total));
+    for (size_t q = 0; q < na; ++q) {
+      const double p = (double)I.last_load[q] * growth;
+      c.push_back({p, I.sub_base + (uint32_t)q, limits[i] - (int)I.tree[(size_t)I.leaves[q]].g});
+      total += p;
     }
   }
+  if (!stat) return;
   const double lanes = s->last_lanes > 0 ? (double)s->last_lanes : (double)s->num_sms * 1024.0;
   const double T = total / (lanes * 4.0);
-  size_t budget = (size_t)1 << 22;
-  plan.max_k = 0;
+  static const size_t pow3[12] = {1, 3, 9, 27, 81, 243, 729, 2187, 6561, 19683, 59049, 177147};
+  auto bound = [&](int kk) { return kk ? 4 * pow3[kk - 1] : (size_t)0; };
   std::vector<int> k(c.size(), 0);
-  if (T > 0 && s->cfg.lb_mode == SP_LB_STATIC_STEAL) {
-    for (size_t j = 0; j < c.size(); ++j) {
+  const int kcap = std::min(10, std::max(1, s->cfg.static_split_cap));
+  size_t need = 0;
+  if (T > 0)
+    for (size_t j = 0; j < c.size(); ++j)
       if (c[j].pred > T) {
         int kk = (int)std::ceil(std::log2(c[j].pred / T));
-        kk = std::min(kk, std::min(10, std::max(0, c[j].room - 1)));
-        k[j] = std::max(0, std::min(kk, std::max(1, s->cfg.static_split_cap)));
+        k[j] = std::max(0, std::min(kk, std::min(kcap, c[j].room - 1)));
+        need += bound(k[j]);
       }
-    }
-    auto bound = [&](int kk) { return kk ? (size_t)4 * (size_t)std::pow(3.0, kk - 1) : 0; };
-    size_t need = 0;
-    for (int kk : k) need += bound(kk);
-    while (need > budget) {  // trim the deepest splits first
-      int mk = 0;
-      for (int kk : k) mk = std::max(mk, kk);
-      if (!mk) break;
-      for (auto &kk : k)
-        if (kk == mk) { need -= bound(kk) - bound(kk - 1); --kk; }
-    }
+  const size_t budget = (size_t)1 << 22;
+  while (need > budget) {  // trim the deepest splits first
+    int mk = 0;
+    for (int kk : k) mk = std::max(mk, kk);
+    if (!mk) break;
+    for (auto &kk : k)
+      if (kk == mk) {
+        need -= bound(kk) - bound(kk - 1);
+        --kk;
+      }
   }
-  std::vector<size_t> order(c.size());
-  for (size_t j = 0; j < c.size(); ++j) order[j] = j;
-  if (s->cfg.lb_mode == SP_LB_STATIC_STEAL)
-    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return c[a].pred > c[b].pred; });
-  std::vector<size_t> level(12, 0);
-  for (size_t j : order) {
+  std::vector<uint32_t> order(c.size());
+  for (size_t j = 0; j < c.size(); ++j) order[j] = (uint32_t)j;
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return c[a].pred > c[b].pred; });
+  size_t level[12] = {0};
+  for (uint32_t j : order) {
     if (k[j] > 0) {
-      Task t = c[j].t;
+      Task t{};
+      t.sub = c[j].sub;
+      t.mask = 0xF;
       t.flags = (uint8_t)k[j];
       plan.split.push_back(t);
       plan.max_k = std::max(plan.max_k, k[j]);
-      for (int l = 1; l <= k[j]; ++l) level[(size_t)l] += (size_t)4 * (size_t)std::pow(3.0, l - 1);
-      plan.emit_bound += (size_t)4 * (size_t)std::pow(3.0, k[j] - 1);
+      for (int l = 1; l <= k[j]; ++l) level[l] += 4 * pow3[l - 1];
+      plan.emit_bound += bound(k[j]);
     } else {
-      plan.direct.push_back(c[j].t);
+      plan.direct.push_back(c[j].sub);
     }
   }
-  for (size_t l = 1; l < level.size(); ++l) plan.level_bound = std::max(plan.level_bound, level[l]);
+  for (int l = 1; l < 12; ++l) plan.level_bound = std::max(plan.level_bound, level[l]);
 }
 
 int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
@@ -532,35 +616,62 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
   for (auto &I : inst) {
     if (I.done) continue;
     std::vector<int32_t> level{0};
-    I.tree[0].leaf = 1;
     for (int dep = 0; dep < 40 && (int)level.size() < target; ++dep) {
       std::vector<int32_t> next;
       for (int32_t x : level) {
-        size_t before = I.tree.size();
+        const size_t before = I.tree.size();
         expand_node(w, I.tree, x);
         for (size_t c = before; c < I.tree.size(); ++c) next.push_back((int32_t)c);
       }
       level.swap(next);
     }
   }
-  std::vector<size_t> from(inst.size(), 0);
-  int rc = compute_tree_h(s, inst, from);
+  int rc = finish_trees(s, inst);
   if (rc) return rc;
-  for (auto &I : inst) {
+  // SubRoot array: the leaves of every instance, in maxf order
+  std::vector<SubRoot> subs;
+  for (size_t i = 0; i < inst.size(); ++i) {
+    Instance &I = inst[i];
+    I.sub_base = (uint32_t)subs.size();
     if (I.done) continue;
-    I.h0 = I.tree[0].h;
-    rebuild_leaves(I);
+    for (int32_t x : I.leaves) {
+      const TreeNode &t = I.tree[(size_t)x];
+      SubRoot r{};
+      memcpy(r.board, t.board, (size_t)n);
+      r.blank = t.blank;
+      r.g = t.g;
+      r.pre = t.pre;
+      r.inst = (uint32_t)i;
+      subs.push_back(r);
+    }
   }
+  const size_t n_subs = subs.size();
+  rc = ensure(s, &s->d_subs, &s->subs_cap, std::max<size_t>(n_subs, 1));
+  if (rc) return rc;
+  rc = ensure(s, &s->d_sub_nodes, &s->sub_nodes_cap, std::max<size_t>(n_subs, 1));
+  if (rc) return rc;
+  if (n_subs) {
+    Pinned<SubRoot> hs;
+    SP_CUDA(s, hs.reserve(n_subs));
+    memcpy(hs.p, subs.data(), n_subs * sizeof(SubRoot));
+    SP_CUDA(s, cudaMemcpyAsync(s->d_subs, hs.p, n_subs * sizeof(SubRoot), cudaMemcpyHostToDevice, s->st));
+    SP_CUDA(s, cudaStreamSynchronize(s->st));
+    s->stats.h2d_bytes += n_subs * sizeof(SubRoot);
+  }
+  if (inst.size() > s->inst_cap || !s->d_limit) {
+    if (s->d_limit) cudaFree(s->d_limit);
+    if (s->d_sol) cudaFree(s->d_sol);
+    s->d_limit = nullptr;
+    s->d_sol = nullptr;
+    const size_t c = std::max<size_t>(inst.size(), 64);
+    SP_CUDA(s, cudaMalloc(&s->d_limit, c * sizeof(int32_t)));
+    SP_CUDA(s, cudaMalloc(&s->d_sol, c * sizeof(Solution)));
+    s->inst_cap = c;
+  }
+  SP_CUDA(s, s->h_limits.reserve(inst.size()));
   s->stats.frontier_ms += ms_since(t_front);
 
-  std::vector<int32_t> sub_base(inst.size(), 0);
-  std::vector<SubRoot> subs;
-  std::vector<Task> init;
   std::vector<int32_t> limits(inst.size(), 0);
-  std::vector<unsigned long long> sub_nodes;
-  std::vector<Solution> sols(inst.size());
-  bool subs_dirty = true;
-
   for (int round = 0; round < SP_MAX_ITERS; ++round) {
     int active = 0;
     for (auto &I : inst) active += !I.done;
@@ -568,141 +679,78 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
     const auto t_round = std::chrono::steady_clock::now();
     const int ri = std::min(round, SP_MAX_ROUNDS - 1);
     s->stats.round_instances[ri] = active;
-    // (re)build the SubRoot array when the trees changed
-    if (subs_dirty) {
-      subs.clear();
-      for (size_t i = 0; i < inst.size(); ++i) {
-        sub_base[i] = (int32_t)subs.size();
-        Instance &I = inst[i];
-        if (I.done) continue;
-        for (int32_t x : I.leaves) {
-          TreeNode &t = I.tree[(size_t)x];
-          t.sub = (int32_t)subs.size();
-          SubRoot r{};
-          memcpy(r.board, t.board, (size_t)n);
-          r.blank = t.blank;
-          r.g = t.g;
-          r.pre = t.pre;
-          r.inst = (uint32_t)i;
-          subs.push_back(r);
-        }
-      }
-      rc = ensure(s, &s->d_subs, &s->subs_cap, std::max<size_t>(subs.size(), 1));
-      if (rc) return rc;
-      if (!subs.empty()) {
-        SP_CUDA(s, cudaMemcpyAsync(s->d_subs, subs.data(), subs.size() * sizeof(SubRoot),
-                                   cudaMemcpyHostToDevice, s->st));
-        s->stats.h2d_bytes += subs.size() * sizeof(SubRoot);
-      }
-      if (s->d_sub_nodes) cudaFree(s->d_sub_nodes);
-      s->d_sub_nodes = nullptr;
-      SP_CUDA(s, cudaMalloc(&s->d_sub_nodes, std::max<size_t>(subs.size(), 1) * sizeof(unsigned long long)));
-      subs_dirty = false;
-    }
-    // per instance: interior counts, host-side goals, active roots
-    std::vector<uint64_t> interior(inst.size(), 0);
-    std::vector<int32_t> host_goal(inst.size(), -1);
     for (size_t i = 0; i < inst.size(); ++i) {
-      Instance &I = inst[i];
-      if (I.done) continue;
-      const int L = I.h0 + 2 * I.iter;
-      limits[i] = L;
-      for (size_t j = 0; j < I.tree.size(); ++j) {
-        const TreeNode &t = I.tree[j];
-        if (t.maxf > L) continue;
-        if (t.h == 0 && (host_goal[i] < 0 || t.g < I.tree[(size_t)host_goal[i]].g)) host_goal[i] = (int32_t)j;
-        if (!t.leaf) interior[i] += t.nchild;
-      }
+      limits[i] = inst[i].done ? -1 : inst[i].h0 + 2 * inst[i].iter;
+      s->h_limits.p[i] = limits[i];
     }
     RoundPlan plan;
-    plan_static(s, inst, limits, plan);
-    const size_t n_tasks = plan.direct.size() + plan.split.size();
-    if (inst.size() > s->inst_cap || !s->d_limit) {
-      if (s->d_limit) cudaFree(s->d_limit);
-      if (s->d_sol) cudaFree(s->d_sol);
-      s->d_limit = nullptr;
-      s->d_sol = nullptr;
-      size_t c = std::max<size_t>(inst.size(), 64);
-      SP_CUDA(s, cudaMalloc(&s->d_limit, c * sizeof(int32_t)));
-      SP_CUDA(s, cudaMalloc(&s->d_sol, c * sizeof(Solution)));
-      s->inst_cap = c;
-    }
-    SP_CUDA(s, cudaMemcpyAsync(s->d_limit, limits.data(), inst.size() * sizeof(int32_t), cudaMemcpyHostToDevice, s->st));
+    plan_round(s, inst, limits, plan);
+    SP_CUDA(s, cudaMemcpyAsync(s->d_limit, s->h_limits.p, inst.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                               s->st));
     SP_CUDA(s, cudaMemsetAsync(s->d_sol, 0, inst.size() * sizeof(Solution), s->st));
-    SP_CUDA(s, cudaMemsetAsync(s->d_sub_nodes, 0, std::max<size_t>(subs.size(), 1) * sizeof(unsigned long long), s->st));
+    SP_CUDA(s, cudaMemsetAsync(s->d_sub_nodes, 0, std::max<size_t>(n_subs, 1) * sizeof(unsigned long long), s->st));
     s->stats.h2d_bytes += inst.size() * sizeof(int32_t);
     float ms = 0;
-    if (n_tasks) {
-      uint32_t split_err = 0;
-      rc = launch_round(s, plan, &ms, &split_err);
+    const unsigned long long *sn = nullptr;
+    const Solution *sols = nullptr;
+    if (!plan.direct.empty() || !plan.split.empty()) {
+      rc = launch_round(s, plan, n_subs, inst.size(), &ms);
       if (rc) return rc;
-      s->stats.kernel_ms += ms;
+      const PoolCtl &ctl = *s->h_ctl.p;
+      fold_ctl(s, ctl, ri, ms);
       s->stats.tasks_initial += plan.direct.size() + s->last_emitted;
-      PoolCtl ctl{};
-      SP_CUDA(s, cudaMemcpyAsync(&ctl, s->d_ctl, sizeof(PoolCtl), cudaMemcpyDeviceToHost, s->st));
-      sub_nodes.assign(subs.size(), 0);
-      SP_CUDA(s, cudaMemcpyAsync(sub_nodes.data(), s->d_sub_nodes, subs.size() * sizeof(unsigned long long),
-                                 cudaMemcpyDeviceToHost, s->st));
-      SP_CUDA(s, cudaMemcpyAsync(sols.data(), s->d_sol, inst.size() * sizeof(Solution), cudaMemcpyDeviceToHost, s->st));
-      SP_CUDA(s, cudaStreamSynchronize(s->st));
-      s->stats.d2h_bytes += sizeof(PoolCtl) + subs.size() * 8 + inst.size() * sizeof(Solution);
-      s->stats.tasks_donated += ctl.donated;
-      s->stats.dev_lane_steps += ctl.counters[0];
-      s->stats.dev_lane_slots += ctl.counters[1];
-      s->stats.dev_idle_cycles += ctl.counters[2];
-      s->stats.dev_warp_cycles += ctl.counters[3];
-      s->stats.dev_donate_tries += ctl.counters[4];
-      s->stats.dev_donate_notfree += ctl.counters[5];
-      s->stats.dev_donate_nowait += ctl.counters[6];
-      s->stats.dev_tasks_done += ctl.counters[7];
       s->stats.round_tasks[ri] = (int32_t)(plan.direct.size() + s->last_emitted);
-      s->stats.round_kernel_ms[ri] = ms;
-      s->stats.round_donated[ri] = ctl.donated;
-      if (!ctl.error && split_err) ctl.error = (int32_t)split_err;
       if (ctl.error) {
         char buf[160];
         snprintf(buf, sizeof buf, "device error %d (info %u) in round %d", ctl.error, ctl.err_info[0], round);
         s->err = buf;
         for (auto &I : inst)
-          if (!I.done) { I.out->status = ctl.error; I.done = true; }
+          if (!I.done) {
+            I.out->status = ctl.error;
+            I.done = true;
+          }
         return ctl.error;
       }
-    } else {
-      sub_nodes.assign(subs.size(), 0);
-      memset(sols.data(), 0, sols.size() * sizeof(Solution));
+      sn = s->h_sub_nodes.p;
+      sols = s->h_sols.p;
     }
     ++s->stats.rounds;
     // fold results
     for (size_t i = 0; i < inst.size(); ++i) {
       Instance &I = inst[i];
       if (I.done) continue;
-      uint64_t nodes = interior[i], dev = 0;
-      for (size_t q = 0; q < I.leaves.size(); ++q) {
-        const uint64_t v = sub_nodes[(size_t)I.tree[(size_t)I.leaves[q]].sub];
+      const int L = limits[i];
+      const size_t na = active_leaves(I, L);
+      uint64_t dev = 0;
+      for (size_t q = 0; q < na; ++q) {
+        const uint64_t v = sn ? sn[I.sub_base + q] : 0;
         dev += v;
         I.last_load[q] = v;
       }
-      nodes += dev;
+      const uint64_t nodes = interior_nodes(I, L) + dev;
       I.prev_total = I.last_total;
       I.last_total = dev;
       sp_result *R = I.out;
-      R->f_limit[I.iter] = limits[i];
+      R->f_limit[I.iter] = L;
       R->nodes[I.iter] = nodes;
       R->nodes_total += nodes;
       R->n_iter = I.iter + 1;
       s->stats.nodes += nodes;
       s->stats.round_nodes[ri] += nodes;
-      const bool dev_goal = sols[i].flag != 0;
-      if (host_goal[i] >= 0 || dev_goal) {
+      int host_goal = -1;
+      for (int32_t x : I.goals) {
+        const TreeNode &t = I.tree[(size_t)x];
+        if (t.maxf <= L && (host_goal < 0 || t.g < I.tree[(size_t)host_goal].g)) host_goal = x;
+      }
+      const bool dev_goal = sols && sols[i].flag != 0;
+      if (host_goal >= 0 || dev_goal) {
         // path: root-set tree prefix, then the device's moves below its root
         std::vector<uint8_t> mv;
-        int node = host_goal[i];
+        int node = host_goal;
         uint32_t extra = 0;
         const uint32_t *pw = nullptr;
         if (node < 0) {
-          const uint32_t sub = sols[i].sub;
-          for (int32_t x : I.leaves)
-            if (I.tree[(size_t)x].sub == (int32_t)sub) node = x;
+          node = I.leaves[sols[i].sub - I.sub_base];
           extra = sols[i].len;
           pw = sols[i].path;
         }
@@ -754,11 +802,11 @@ void sp_config_default(sp_config *c) {
   c->frontier_target = 2048;
   c->threads_per_block = 256;
   c->blocks_per_sm = 0;
-  c->lb_mode = SP_LB_STEAL;
+  c->lb_mode = SP_LB_STATIC_STEAL;
   c->donate_min_slack = 6;
   c->steps_per_poll = 32;
   c->timeout_ms = 20000;
-  c->static_split_cap = 64;
+  c->static_split_cap = 10;
 }
 
 int sp_create(int width, int heuristic, const sp_config *cfg, sp_solver **out) {
@@ -806,7 +854,7 @@ void sp_destroy(sp_solver *s) {
   cudaFree(s->d_seq);
   cudaFree(s->d_ctl);
   cudaFree(s->d_subs);
-  cudaFree(s->d_init);
+  cudaFree(s->d_direct);
   cudaFree(s->d_sub_nodes);
   cudaFree(s->d_limit);
   cudaFree(s->d_sol);
@@ -893,18 +941,18 @@ int sp_heuristic(sp_solver *s, const uint8_t *tiles, int n, int32_t *h) {
   if (s->heur == SP_HEUR_PDB && !s->pdb_ready) return SP_ERR_NO_PDB;
   if (n == 0) return SP_OK;
   for (int i = 0; i < n; ++i) {
-    int st = check_instance(s->w, tiles + (size_t)i * s->n);
+    const int st = check_instance(s->w, tiles + (size_t)i * s->n);
     if (st == SP_ERR_NOT_PERMUTATION) return st;
   }
   int rc = ensure(s, &s->d_boards, &s->boards_cap, (size_t)n * s->n);
   if (rc) return rc;
-  int32_t *dh = nullptr;
-  SP_CUDA(s, cudaMalloc(&dh, (size_t)n * sizeof(int32_t)));
+  rc = ensure(s, &s->d_h, &s->h_cap, (size_t)n);
+  if (rc) return rc;
   cudaError_t e = cudaMemcpyAsync(s->d_boards, tiles, (size_t)n * s->n, cudaMemcpyHostToDevice, s->st);
-  if (e == cudaSuccess) e = launch_heuristic(s->w, s->heur == SP_HEUR_PDB, s->d_boards, n, dh, s->d_ht, s->d_pdb, s->st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(h, dh, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, s->st);
+  if (e == cudaSuccess)
+    e = launch_heuristic(s->w, s->heur == SP_HEUR_PDB, s->d_boards, n, s->d_h, s->d_ht, s->d_pdb, s->st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, s->d_h, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, s->st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
-  cudaFree(dh);
   if (e != cudaSuccess) return fail_cuda(s, e, "sp_heuristic");
   return SP_OK;
 }
@@ -921,7 +969,7 @@ int sp_solve_batch_device(sp_solver *s, const void *d_tiles, int n, sp_result *r
   std::vector<uint8_t> h((size_t)n * s->n);
   SP_CUDA(s, cudaMemcpyAsync(h.data(), d_tiles, h.size(), cudaMemcpyDeviceToHost, s->st));
   SP_CUDA(s, cudaStreamSynchronize(s->st));
-  int rc = solve_impl(s, h.data(), n, results);
+  const int rc = solve_impl(s, h.data(), n, results);
   s->stats.d2h_bytes += h.size();
   return rc;
 }
@@ -934,7 +982,8 @@ int sp_dfs_round(sp_solver *s, const uint8_t *roots, const int32_t *depth, const
   *found = -1;
   if (n == 0) return SP_OK;
   std::vector<SubRoot> subs((size_t)n);
-  std::vector<Task> init((size_t)n);
+  RoundPlan plan;
+  plan.direct.resize((size_t)n);
   for (int i = 0; i < n; ++i) {
     const uint8_t *t = roots + (size_t)i * s->n;
     if (check_instance(s->w, t) == SP_ERR_NOT_PERMUTATION) return SP_ERR_NOT_PERMUTATION;
@@ -947,12 +996,10 @@ int sp_dfs_round(sp_solver *s, const uint8_t *roots, const int32_t *depth, const
     r.pre = pre[i] < 0 ? kNoPre : (uint8_t)pre[i];
     r.inst = 0;
     subs[(size_t)i] = r;
-    init[(size_t)i].sub = (uint32_t)i;
-    init[(size_t)i].plen = 0;
-    init[(size_t)i].mask = 0xF;
+    plan.direct[(size_t)i] = (uint32_t)i;
   }
-  // roots that are goals within the limit (the reference's dfs_kernel sets
-  // dev_flag for them, :580-583)
+  // roots that are goals (the reference's dfs_kernel sets dev_flag for them,
+  // src/24puzzle_block_parallel_with_pdb.cu:580-583)
   std::vector<int32_t> h((size_t)n);
   int rc = sp_heuristic(s, roots, n, h.data());
   if (rc) return rc;
@@ -960,45 +1007,26 @@ int sp_dfs_round(sp_solver *s, const uint8_t *roots, const int32_t *depth, const
     if (h[(size_t)i] == 0 && (*found < 0 || depth[i] < *found)) *found = depth[i];
   rc = ensure(s, &s->d_subs, &s->subs_cap, (size_t)n);
   if (rc) return rc;
+  rc = ensure(s, &s->d_sub_nodes, &s->sub_nodes_cap, (size_t)n);
+  if (rc) return rc;
   if (!s->d_limit || s->inst_cap < 1) {
     SP_CUDA(s, cudaMalloc(&s->d_limit, 64 * sizeof(int32_t)));
     SP_CUDA(s, cudaMalloc(&s->d_sol, 64 * sizeof(Solution)));
     s->inst_cap = 64;
   }
-  if (s->d_sub_nodes) cudaFree(s->d_sub_nodes);
-  s->d_sub_nodes = nullptr;
-  SP_CUDA(s, cudaMalloc(&s->d_sub_nodes, (size_t)n * sizeof(unsigned long long)));
   SP_CUDA(s, cudaMemcpyAsync(s->d_subs, subs.data(), subs.size() * sizeof(SubRoot), cudaMemcpyHostToDevice, s->st));
   SP_CUDA(s, cudaMemcpyAsync(s->d_limit, &limit, sizeof(int32_t), cudaMemcpyHostToDevice, s->st));
   SP_CUDA(s, cudaMemsetAsync(s->d_sol, 0, sizeof(Solution), s->st));
   SP_CUDA(s, cudaMemsetAsync(s->d_sub_nodes, 0, (size_t)n * sizeof(unsigned long long), s->st));
   float ms = 0;
-  RoundPlan plan;
-  plan.direct = std::move(init);
-  uint32_t split_err = 0;
-  rc = launch_round(s, plan, &ms, &split_err);
+  rc = launch_round(s, plan, (size_t)n, 1, &ms);
   if (rc) return rc;
-  PoolCtl ctl{};
-  Solution sol{};
-  SP_CUDA(s, cudaMemcpyAsync(&ctl, s->d_ctl, sizeof(PoolCtl), cudaMemcpyDeviceToHost, s->st));
-  SP_CUDA(s, cudaMemcpyAsync(&sol, s->d_sol, sizeof(Solution), cudaMemcpyDeviceToHost, s->st));
-  SP_CUDA(s, cudaMemcpyAsync(nodes, s->d_sub_nodes, (size_t)n * sizeof(uint64_t), cudaMemcpyDeviceToHost, s->st));
-  SP_CUDA(s, cudaStreamSynchronize(s->st));
-  s->stats.kernel_ms = ms;
+  const PoolCtl &ctl = *s->h_ctl.p;
+  memcpy(nodes, s->h_sub_nodes.p, (size_t)n * sizeof(uint64_t));
+  fold_ctl(s, ctl, 0, ms);
   s->stats.rounds = 1;
   s->stats.tasks_initial = (uint64_t)n;
-  s->stats.tasks_donated = ctl.donated;
-  s->stats.dev_lane_steps = ctl.counters[0];
-  s->stats.dev_lane_slots = ctl.counters[1];
-  s->stats.dev_idle_cycles = ctl.counters[2];
-  s->stats.dev_warp_cycles = ctl.counters[3];
-  s->stats.dev_donate_tries = ctl.counters[4];
-  s->stats.dev_donate_notfree = ctl.counters[5];
-  s->stats.dev_donate_nowait = ctl.counters[6];
-  s->stats.dev_tasks_done = ctl.counters[7];
   s->stats.round_tasks[0] = n;
-  s->stats.round_kernel_ms[0] = ms;
-  s->stats.round_donated[0] = ctl.donated;
   if (ctl.error) {
     char buf[320];
     snprintf(buf, sizeof buf,
@@ -1010,6 +1038,7 @@ int sp_dfs_round(sp_solver *s, const uint8_t *roots, const int32_t *depth, const
     s->err = buf;
     return ctl.error;
   }
+  const Solution &sol = s->h_sols.p[0];
   if (sol.flag) {
     const int d = (int)subs[sol.sub].g + (int)sol.len;
     if (*found < 0 || d < *found) *found = d;

@@ -35,7 +35,7 @@ cudaError_t launch_search_round(int w, bool pdb, int block, int blocks_per_sm, i
                                 const RoundParams &P, cudaStream_t st, int *grid_out);
 // Publish the round's tasks (split pieces first, then the direct tasks) and
 // reset the pool control block.
-cudaError_t launch_pool_init(Task *tasks, const Task *emit, const uint32_t *n_emit, const Task *direct,
+cudaError_t launch_pool_init(Task *tasks, const Task *emit, const uint32_t *n_emit, const uint32_t *direct,
                              uint32_t n_direct, uint32_t *seq, uint32_t cap, PoolCtl *ctl, cudaStream_t st);
 
 // Split pre-pass: one breadth-first level over `in` (count *n_in).
