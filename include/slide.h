@@ -75,7 +75,9 @@ typedef struct {
   int32_t donate_min_slack;  /* donate a branch only if limit - depth >= this */
   int32_t steps_per_poll;    /* DFS steps between task-pool polls */
   int32_t timeout_ms;        /* device no-progress limit for pool waits */
-  int32_t static_split_cap;  /* max pieces one root is split into (static LB) */
+  int32_t static_split_cap;  /* max levels a root is split by (static LB) */
+  int32_t donate_reserve;    /* donate while fewer tasks than this are queued;
+                                0 = resident lanes / 16, -1 = only when a lane waits */
 } sp_config;
 
 /* One instance's answer: "state in, optimal move sequence and per-iteration

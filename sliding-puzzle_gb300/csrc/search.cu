@@ -489,26 +489,40 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
         }
       }
     }
-    // 5. donate while someone waits (head ahead of tail)
-    if (P.donate && hd > tl) {
+    // 5. donate while fewer than `reserve` tasks are queued (tail - head)
+    if (P.donate && hd + P.reserve > tl) {
       uint32_t dmask = 0;
       int lev = (state == 2) ? find_donation(dmask) : -1;
       if (lev >= 0 && plen + lev > kMaxPath) lev = -1;  // prefix would not fit a record
-      // one donor per warp per poll: the lane with the shallowest level
-      const unsigned key = lev >= 0 ? ((unsigned)lev << 5) | (unsigned)lane : 0xFFFFFFFFu;
+      // donors: lanes whose open level is within one of the warp's shallowest,
+      // at most `allowed` of them (more when the shortfall is large)
+      const unsigned key = lev >= 0 ? (unsigned)lev : 0xFFFFFFFFu;
       const unsigned best = __reduce_min_sync(FULL, key);
+      const uint32_t shortfall = hd + P.reserve - tl;
+      const unsigned allowed = min(8u, 1u + shortfall / P.spread);
+      const unsigned cand = __ballot_sync(FULL, lev >= 0 && (unsigned)lev <= best + 1u);
+      const unsigned rank = __popc(cand & ((1u << lane) - 1u));
+      const bool donor = ((cand >> lane) & 1u) && rank < allowed;
+      const unsigned donors = __ballot_sync(FULL, donor);
       if (lane == 0) {
         ++c_nowait;  // hungry polls
-        if (best != 0xFFFFFFFFu) ++c_found;
+        if (donors) ++c_found;
       }
-      if (best != 0xFFFFFFFFu && (int)(best & 31u) == lane) {
-        // reserve the next index; its ring slot is free once the slot's previous
+      uint32_t tbase = 0;
+      const int lead = donors ? __ffs(donors) - 1 : 0;
+      if (donors && lane == lead) {
+        tbase = atomicAdd(&ctl->tail, (uint32_t)__popc(donors));
+        atomicAdd(&ctl->outstanding, (uint32_t)__popc(donors));
+      }
+      tbase = __shfl_sync(FULL, tbase, lead);
+      if (donor) {
+        // the reserved index's ring slot is free once the slot's previous
         // occupant (index t - cap, claimed long before) was copied out, which
         // in practice it already is -- wait a bounded time, else leave the
         // index unpublished (its claimant then idles until the round ends)
         const uint32_t mask = P.cap - 1u;
         ++c_tries;
-        const uint32_t t = atomicAdd(&ctl->tail, 1u);
+        const uint32_t t = tbase + (uint32_t)__popc(donors & ((1u << lane) - 1u));
         bool ok = false;
         for (int spin = 0; spin < 4096; ++spin) {
           if (ld_acquire(&P.seq[t & mask]) == t) {
@@ -517,9 +531,11 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
           }
           __nanosleep(64);
         }
-        if (!ok) ++c_notfree;
+        if (!ok) {
+          ++c_notfree;
+          atomicSub(&ctl->outstanding, 1u);  // nothing published at t
+        }
         if (ok) {
-          atomicAdd(&ctl->outstanding, 1u);
           Task *D = &P.tasks[t & mask];
           const int nlen = plen + lev;
           D->sub = sub;

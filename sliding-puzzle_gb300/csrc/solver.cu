@@ -164,6 +164,9 @@ struct sp_solver {
   Pinned<PoolCtl> h_ctl;
   Pinned<int32_t> h_limits;
   Pinned<uint32_t> h_cnt;
+  Pinned<uint8_t> h_boards;
+  Pinned<int32_t> h_hv;
+  Pinned<SubRoot> h_subs;
   std::string err;
   sp_stats stats{};
 };
@@ -280,8 +283,8 @@ int finish_trees(sp_solver *s, std::vector<Instance> &inst) {
   if (rc) return rc;
   rc = ensure(s, &s->d_h, &s->h_cap, total);
   if (rc) return rc;
-  Pinned<uint8_t> boards;
-  Pinned<int32_t> hv;
+  Pinned<uint8_t> &boards = s->h_boards;
+  Pinned<int32_t> &hv = s->h_hv;
   SP_CUDA(s, boards.reserve(total * (size_t)s->n));
   SP_CUDA(s, hv.reserve(total));
   size_t o = 0;
@@ -482,6 +485,10 @@ int launch_round(sp_solver *s, const RoundPlan &plan, size_t n_subs, size_t n_in
   P.timeout_ns = (unsigned long long)s->cfg.timeout_ms * 1000000ull;
   P.poll_ns = 2000;
   const int block = s->cfg.threads_per_block == 128 ? 128 : 256;
+  const uint32_t lanes = (uint32_t)(s->last_lanes > 0 ? s->last_lanes : s->num_sms * 1024);
+  P.reserve = s->cfg.donate_reserve < 0 ? 0u : s->cfg.donate_reserve > 0 ? (uint32_t)s->cfg.donate_reserve
+                                                                          : lanes / 16u;
+  P.spread = std::max(1u, lanes / 32u);
   int grid = 0;
   SP_CUDA(s, launch_search_round(s->w, s->heur == SP_HEUR_PDB, block, s->cfg.blocks_per_sm, s->num_sms, P,
                                  s->st, &grid));
@@ -547,13 +554,21 @@ void plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int
   std::vector<int> k(c.size(), 0);
   const int kcap = std::min(10, std::max(1, s->cfg.static_split_cap));
   size_t need = 0;
-  if (T > 0)
-    for (size_t j = 0; j < c.size(); ++j)
-      if (c[j].pred > T) {
-        int kk = (int)std::ceil(std::log2(c[j].pred / T));
-        k[j] = std::max(0, std::min(kk, std::min(kcap, c[j].room - 1)));
-        need += bound(k[j]);
-      }
+  // exponent of pred relative to T (ceil(log2(pred/T)) for pred > T), also the
+  // bucket of the longest-first order
+  std::vector<int8_t> ex(c.size(), 0);
+  for (size_t j = 0; j < c.size(); ++j) {
+    int e = -64;
+    if (c[j].pred > 0 && T > 0) {
+      std::frexp(c[j].pred / T, &e);  // pred/T in [2^(e-1), 2^e)
+      e = std::max(-63, std::min(63, e));
+    }
+    ex[j] = (int8_t)e;
+    if (T > 0 && c[j].pred > T) {
+      k[j] = std::max(0, std::min(e, std::min(kcap, c[j].room - 1)));
+      need += bound(k[j]);
+    }
+  }
   const size_t budget = (size_t)1 << 22;
   while (need > budget) {  // trim the deepest splits first
     int mk = 0;
@@ -565,9 +580,14 @@ void plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int
         --kk;
       }
   }
+  // longest first: counting sort on the exponent (descending), stable within
   std::vector<uint32_t> order(c.size());
-  for (size_t j = 0; j < c.size(); ++j) order[j] = (uint32_t)j;
-  std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return c[a].pred > c[b].pred; });
+  {
+    size_t cnt[129] = {0};
+    for (int8_t e : ex) ++cnt[63 - e + 1];
+    for (int b = 1; b < 129; ++b) cnt[b] += cnt[b - 1];
+    for (size_t j = 0; j < c.size(); ++j) order[cnt[63 - ex[j]]++] = (uint32_t)j;
+  }
   size_t level[12] = {0};
   for (uint32_t j : order) {
     if (k[j] > 0) {
@@ -651,7 +671,7 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
   rc = ensure(s, &s->d_sub_nodes, &s->sub_nodes_cap, std::max<size_t>(n_subs, 1));
   if (rc) return rc;
   if (n_subs) {
-    Pinned<SubRoot> hs;
+    Pinned<SubRoot> &hs = s->h_subs;
     SP_CUDA(s, hs.reserve(n_subs));
     memcpy(hs.p, subs.data(), n_subs * sizeof(SubRoot));
     SP_CUDA(s, cudaMemcpyAsync(s->d_subs, hs.p, n_subs * sizeof(SubRoot), cudaMemcpyHostToDevice, s->st));
@@ -790,7 +810,7 @@ bool config_ok(const sp_config *c) {
          c->frontier_target <= (1 << 20) && c->blocks_per_sm >= 0 && c->blocks_per_sm <= 16 &&
          c->lb_mode >= SP_LB_STEAL && c->lb_mode <= SP_LB_NONE && c->donate_min_slack >= 0 &&
          c->steps_per_poll >= 1 && c->steps_per_poll <= 4096 && c->timeout_ms >= 100 &&
-         c->timeout_ms <= 600000 && c->static_split_cap >= 1;
+         c->timeout_ms <= 600000 && c->static_split_cap >= 1 && c->donate_reserve >= -1;
 }
 
 }  // namespace
@@ -807,6 +827,7 @@ void sp_config_default(sp_config *c) {
   c->steps_per_poll = 32;
   c->timeout_ms = 20000;
   c->static_split_cap = 10;
+  c->donate_reserve = 0;
 }
 
 int sp_create(int width, int heuristic, const sp_config *cfg, sp_solver **out) {

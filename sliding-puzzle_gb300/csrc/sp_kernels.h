@@ -25,7 +25,9 @@ struct RoundParams {
   int32_t min_slack;
   int32_t steps;
   int32_t donate;
-  int32_t pad;
+  uint32_t reserve;   // donate while fewer than this many tasks are queued
+  uint32_t spread;    // one extra donor per warp per `spread` missing tasks
+  uint32_t pad1;
   unsigned long long timeout_ns;
   unsigned long long poll_ns;  // min interval of a block's global pool poll
 };
