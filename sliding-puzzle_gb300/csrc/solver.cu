@@ -31,6 +31,7 @@
 #include <cstdio>
 #include <memory>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/slide.h"
@@ -267,6 +268,24 @@ void expand_node(int w, std::vector<TreeNode> &tree, int idx) {
   tree[(size_t)idx].leaf = 0;
 }
 
+// fn(i) for i in [0, n) on up to 16 host threads (instances are independent)
+template <typename F>
+void parallel_for(size_t n, F fn) {
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const unsigned nt = (unsigned)std::min<size_t>(hw, std::max<size_t>(1, n / 4));
+  if (nt <= 1) {
+    for (size_t i = 0; i < n; ++i) fn(i);
+    return;
+  }
+  std::atomic<size_t> next{0};
+  std::vector<std::thread> pool;
+  for (unsigned t = 0; t < nt; ++t)
+    pool.emplace_back([&]() {
+      for (size_t i; (i = next.fetch_add(1)) < n;) fn(i);
+    });
+  for (auto &th : pool) th.join();
+}
+
 uint8_t count_children(int w, const TreeNode &t) {
   uint32_t mv = legal_moves(w, t.blank);
   if (t.pre != kNoPre) mv &= ~(1u << (3 - t.pre));
@@ -297,15 +316,18 @@ int finish_trees(sp_solver *s, std::vector<Instance> &inst) {
   SP_CUDA(s, cudaMemcpyAsync(hv.p, s->d_h, total * sizeof(int32_t), cudaMemcpyDeviceToHost, s->st));
   SP_CUDA(s, cudaStreamSynchronize(s->st));
   s->stats.d2h_bytes += total * sizeof(int32_t);
-  o = 0;
-  for (auto &I : inst) {
+  std::vector<size_t> first(inst.size() + 1, 0);
+  for (size_t i = 0; i < inst.size(); ++i) first[i + 1] = first[i] + inst[i].tree.size();
+  parallel_for(inst.size(), [&](size_t i) {
+    Instance &I = inst[i];
+    size_t o = first[i];
     for (auto &t : I.tree) {
       t.h = hv.p[o++];
       const int f = (int)t.g + t.h;
       t.maxf = t.parent < 0 ? f : std::max(I.tree[(size_t)t.parent].maxf, f);
       t.nchild = count_children(s->w, t);
     }
-    if (I.done) continue;
+    if (I.done) return;
     I.h0 = I.tree[0].h;
     I.leaves.clear();
     std::vector<std::pair<int32_t, uint8_t>> interior;
@@ -328,7 +350,7 @@ int finish_trees(sp_solver *s, std::vector<Instance> &inst) {
       else I.interior.push_back({x.first, cum});
     }
     I.last_load.assign(I.leaves.size(), 0);
-  }
+  });
   return SP_OK;
 }
 
@@ -630,14 +652,18 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
     make_root(w, tiles + (size_t)i * n, &root);
     I.tree.push_back(root);
   }
-  // root set: uniform-depth tree expansion to >= frontier_target leaves
+  // root set: uniform-depth tree expansion to >= frontier_target leaves,
+  // instances spread over host threads
   auto t_front = std::chrono::steady_clock::now();
   const int target = std::max(1, s->cfg.frontier_target);
-  for (auto &I : inst) {
-    if (I.done) continue;
-    std::vector<int32_t> level{0};
+  auto build_tree = [&](Instance &I) {
+    if (I.done) return;
+    I.tree.reserve((size_t)target * 4 + 16);
+    std::vector<int32_t> level{0}, next;
+    level.reserve((size_t)target * 4);
+    next.reserve((size_t)target * 4);
     for (int dep = 0; dep < 40 && (int)level.size() < target; ++dep) {
-      std::vector<int32_t> next;
+      next.clear();
       for (int32_t x : level) {
         const size_t before = I.tree.size();
         expand_node(w, I.tree, x);
@@ -645,7 +671,8 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
       }
       level.swap(next);
     }
-  }
+  };
+  parallel_for(inst.size(), [&](size_t i) { build_tree(inst[i]); });
   int rc = finish_trees(s, inst);
   if (rc) return rc;
   // SubRoot array: the leaves of every instance, in maxf order
