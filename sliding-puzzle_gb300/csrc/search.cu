@@ -290,6 +290,7 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
   };
   auto record_goal = [&]() {
     Solution *S = &P.sol[P.subs[sub].inst];
+    atomicMax(&S->best, 0xFFFFFFFFu - (uint32_t)g);  // shortest goal depth over all lanes
     if (atomicCAS(&S->flag, 0u, 1u) == 0u) {
       int len = plen + k;
       S->sub = sub;
@@ -664,6 +665,7 @@ __global__ void split_level_kernel(SplitArgs A) {
       C.flags = (uint8_t)(T.flags - 1);
       if (hc == 0) {  // a goal at the child: record it like the search does
         Solution *S = &A.sol[R.inst];
+        atomicMax(&S->best, 0xFFFFFFFFu - (uint32_t)(g + 1));
         if (atomicCAS(&S->flag, 0u, 1u) == 0u) {
           S->sub = T.sub;
           S->len = (uint32_t)(q + 1);

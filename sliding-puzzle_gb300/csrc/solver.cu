@@ -1087,8 +1087,8 @@ int sp_dfs_round(sp_solver *s, const uint8_t *roots, const int32_t *depth, const
     return ctl.error;
   }
   const Solution &sol = s->h_sols.p[0];
-  if (sol.flag) {
-    const int d = (int)subs[sol.sub].g + (int)sol.len;
+  if (sol.flag && sol.best) {
+    const int d = (int)(0xFFFFFFFFu - sol.best);
     if (*found < 0 || d < *found) *found = d;
   }
   for (int i = 0; i < n; ++i) s->stats.nodes += nodes[i];

@@ -102,12 +102,14 @@ struct Task {
 };
 static_assert(sizeof(Task) == 48, "Task layout");
 
-// One goal per instance: moves below its SubRoot.
+// One goal per instance: moves below its SubRoot.  `best` is
+// 0xFFFFFFFF - (shortest absolute goal depth seen), 0 when none, so that a
+// zeroed record needs no further initialisation.
 struct Solution {
   uint32_t flag;
   uint32_t sub;
   uint32_t len;
-  uint32_t pad;
+  uint32_t best;
   uint32_t path[kPathWords];
   uint32_t pad2[2];
 };
