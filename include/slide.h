@@ -174,6 +174,24 @@ int sp_dfs_round(sp_solver *s, const uint8_t *roots, const int32_t *depth,
                  const int32_t *pre, int n, int limit, uint64_t *nodes,
                  int32_t *found);
 
+/* sp_dfs_round for the Manhattan heuristic without allocating any memory.
+ * No counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc (code inside a stream capture that must stay free of allocation
+ * nodes, hosts whose framework owns the device allocator, real-time loops
+ * that must not enter the driver's allocator).  All pointers are device
+ * pointers owned by the caller: d_roots n*width*width tiles, d_depth[n],
+ * d_pre[n] as in sp_dfs_round, d_nodes[n] and d_found[1] receive its
+ * outputs; stream is a cudaStream_t (NULL = default stream) and the call
+ * returns after the stream has drained.  Scratch lives in a fixed device
+ * array of about 7 MB that every GPU loading the library keeps until exit;
+ * n above 16384 roots returns SP_ERR_CAPACITY.  Calls share that array:
+ * calls overlapping on the GPU race, so serialise them.  The first call on a
+ * device sets the array up (cudaGetSymbolAddress, table copy): make it before
+ * any stream capture begins. */
+int sp_dfs_round_md_noalloc(int width, const uint8_t *d_roots, const int32_t *d_depth,
+                            const int32_t *d_pre, int n, int limit, uint64_t *d_nodes,
+                            int32_t *d_found, void *stream);
+
 int sp_last_stats(const sp_solver *s, sp_stats *out);
 const char *sp_status_string(int status);
 const char *sp_last_error(const sp_solver *s);
