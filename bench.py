@@ -155,8 +155,39 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_probe(args):
+    """Steady-state kernel probe: one root replicated `--roots` times in one
+    threshold round (identical subtrees, so no load imbalance)."""
+    import torch
+    import instances
+    import slide
+    torch.cuda.set_device(0)
+    width = 4 if args.probe_width == 4 else 5
+    s = slide.Solver(width, args.probe_heuristic)
+    if args.probe_heuristic == "pdb":
+        s.build_pdb()
+    root = instances.random_walks(width, 1, 50, seed=5)
+    h0 = int(s.heuristic_values(root)[0])
+    n = args.roots
+    roots = np.repeat(root, n, axis=0)
+    zeros, pre = np.zeros(n, np.int32), -np.ones(n, np.int32)
+    s.dfs_round(roots[:1024], zeros[:1024], pre[:1024], h0 + args.probe_slack)  # warm-up
+    nodes, _ = s.dfs_round(roots, zeros, pre, h0 + args.probe_slack)
+    x = s.stats()
+    print(json.dumps({"probe": "balanced", "width": width, "heuristic": args.probe_heuristic, "roots": n,
+                      "nodes_per_root": int(nodes[0]), "kernel_ms": x["kernel_ms"],
+                      "nodes_per_s": float(nodes.sum()) / (x["kernel_ms"] / 1000.0),
+                      "lane_step_fraction": x["dev_lane_steps"] / max(1, x["dev_lane_slots"]),
+                      "idle_fraction": x["dev_idle_cycles"] / max(1, x["dev_warp_cycles"])}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--probe", choices=["balanced"], default=None)
+    ap.add_argument("--probe-heuristic", default="pdb", choices=["manhattan", "pdb"])
+    ap.add_argument("--probe-width", type=int, default=4)
+    ap.add_argument("--probe-slack", type=int, default=8)
+    ap.add_argument("--roots", type=int, default=100000)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -168,6 +199,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
+    if args.probe:
+        return run_probe(args)
     if args.impl == "reference":
         return run_reference(args)
 
@@ -262,10 +295,12 @@ def main():
     peak, peak_kind = load_peaks()
     kms = sum(kern_ms)
     achieved = nodes * BYTES_PER_NODE / (kms / 1000.0) / 1e9 if kms > 0 else 0.0
-    traffic = None
-    prof = os.path.join(ROOT, "profiles", "search_round_pdb15_traffic.json")
+    traffic = None  # DRAM bytes per search launch, from the committed ncu summary
+    prof = os.path.join(ROOT, "profiles", "search_round_pdb15_random100.md")
     if os.path.exists(prof):
-        traffic = json.load(open(prof)).get("bytes_per_launch")
+        for line in open(prof):
+            if line.startswith("traffic_bytes_per_launch:"):
+                traffic = float(line.split(":")[1])
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_sample(w, states, budget_s=args.cpu_seconds, threads=os.cpu_count() or 1)
