@@ -78,6 +78,8 @@ typedef struct {
   int32_t static_split_cap;  /* max levels a root is split by (static LB) */
   int32_t donate_reserve;    /* donate while fewer tasks than this are queued;
                                 0 = resident lanes / 16, -1 = only when a lane waits */
+  int32_t persistent;        /* 1: every instance's threshold loop runs on the device in
+                                one launch; 0: one launch per threshold round */
 } sp_config;
 
 /* One instance's answer: "state in, optimal move sequence and per-iteration

@@ -28,6 +28,12 @@
 //    :200-247; the reference's own balance is the host re-split of
 //    :839-897, done by the host round loop here).
 //
+// The multi-iteration variant (MULTI) runs every instance's whole threshold
+// loop in one launch: the warp whose lane finishes an instance's last task of
+// an iteration publishes that instance's next iteration (warp_advance), so
+// instances never wait for each other and the host is not involved between
+// iterations.
+//
 // Every wait is bounded: a warp whose lanes all wait and see no change of the
 // pool for timeout_ns sets SP_ERR_TIMEOUT and every warp returns.  Nothing
 // traps.
@@ -106,8 +112,142 @@ __device__ __forceinline__ uint32_t set_byte(uint32_t v, int p, uint32_t x) {
 
 }  // namespace
 
-template <int W, bool PDB, int BLOCK, int WORDS>
-__global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
+// Multi-iteration mode: the warp of the lane that finished an instance's last
+// task of an iteration completes that iteration (adds the root-set interior
+// count, checks for a goal) and publishes the next iteration's roots -- the
+// threshold loop of src/24puzzle_block_parallel_with_pdb.cu:772-921 run on the
+// device, per instance, with no barrier across instances.  Called by all 32
+// lanes of a warp with the same instance i; `hist` is the warp's 32 words of
+// shared memory.  Kept out of line: it is cold, and inlined its registers
+// would crowd the search loop.
+#ifndef SP_MULTI_PIECE
+#define SP_MULTI_PIECE 1.0  // split-piece load in units of the instance's average root load
+#endif
+__device__ __noinline__ void warp_advance(const RoundParams &P, uint32_t i, uint32_t *hist) {
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  PoolCtl *ctl = P.ctl;
+  auto interior = [&](int L) -> unsigned long long {
+    const uint32_t off = P.inter_off[i];
+    int lo = 0, hi = (int)P.inter_len[i];  // first entry with f > L
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (P.inter_f[off + mid] <= L) lo = mid + 1;
+      else hi = mid;
+    }
+    return lo ? P.inter_cum[off + lo - 1] : 0ull;
+  };
+  int r = ld_volatile(&P.inst_iter[i]);
+  int L = ld_volatile(&P.inst_limit[i]);
+  if (lane == 0) atomicAdd(&P.iter_nodes[(size_t)i * kMaxIters + r], interior(L));
+  for (;;) {
+    // every task of iteration r has finished: the goal flag is final
+    int stop = 0;
+    if (lane == 0) stop = (ld_volatile(&P.sol[i].flag) != 0u || P.goal_maxf[i] <= L) ? 1 : 0;
+    stop = __shfl_sync(FULL, stop, 0);
+    if (stop || r + 1 >= kMaxIters) {
+      if (lane == 0) {
+        P.inst_final[i] = r;
+        if (!stop) P.inst_status[i] = SP_ERR_LIMIT;
+      }
+      return;
+    }
+    ++r;
+    L += 2;
+    const uint32_t base = P.inst_sub_base[i], ns = P.inst_nsub[i];
+    uint32_t lo = 0, hi = ns;  // active roots: prefix with maxf <= L
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (P.sub_maxf[base + mid] <= L) lo = mid + 1;
+      else hi = mid;
+    }
+    const uint32_t na = lo;
+    if (lane == 0) {
+      P.inst_iter[i] = r;
+      const_cast<int32_t *>(P.inst_limit)[i] = L;
+      if (!na) atomicAdd(&P.iter_nodes[(size_t)i * kMaxIters + r], interior(L));
+    }
+    if (!na) continue;
+    // loads of iteration r - 1 (summed by atomics in L2: read past L1)
+    const unsigned long long *ld = P.sub_loads + (size_t)((r - 1) & 1) * P.n_subs + base;
+    unsigned long long *nx = P.sub_loads + (size_t)(r & 1) * P.n_subs + base;
+    unsigned long long tot = 0;
+    for (uint32_t q = lane; q < na; q += 32) tot += __ldcg(ld + q);
+    for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
+    const double avg = (double)tot / (double)na;
+    for (uint32_t q = lane; q < ns; q += 32) nx[q] = 0;
+    // longest first: bucket = binary exponent of load / average (0 = no load)
+    auto bucket = [&](double lq) -> int {
+      if (!(lq > 0.0) || !(avg > 0.0)) return 0;
+      int e = 0;
+      frexp(lq / avg, &e);
+      return min(31, max(1, e + 15));
+    };
+    hist[lane] = 0;
+    __syncwarp();
+    for (uint32_t q = lane; q < na; q += 32) atomicAdd(&hist[bucket((double)__ldcg(ld + q))], 1u);
+    __syncwarp();
+    const uint32_t c = hist[lane];
+    uint32_t suf = c;  // roots in buckets >= lane
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t v = __shfl_down_sync(FULL, suf, o);
+      if (lane + o < 32) suf += v;
+    }
+    hist[lane] = suf - c;  // first position of bucket `lane`
+    // the whole iteration is outstanding before its first task is visible
+    uint32_t t0 = 0;
+    if (lane == 0) {
+      atomicAdd(&P.inst_out[i], na);
+      atomicAdd(&ctl->outstanding, na);
+      t0 = atomicAdd(&ctl->tail, na);
+      __threadfence();
+    }
+    t0 = __shfl_sync(FULL, t0, 0);
+    __syncwarp();
+    const uint32_t mask = P.cap - 1u;
+    for (uint32_t q = lane; q < na; q += 32) {
+      const double lq = (double)__ldcg(ld + q);
+      const uint32_t t = t0 + atomicAdd(&hist[bucket(lq)], 1u);
+      int kk = 0;
+      const double piece = avg * SP_MULTI_PIECE;
+      if (P.static_split && piece > 0 && lq > 2.0 * piece) {
+        // static split from the loads just measured: a root with x pieces'
+        // load goes out as a split task of about log(x)/log(2.4) levels (the
+        // reference cuts it into ceil(load/avg) pieces,
+        // src/24puzzle_block_parallel_with_pdb.cu:839-897)
+        kk = (int)ceil(log(lq / piece) / log(2.4));
+        kk = max(0, min(kk, min(10, L - (int)P.subs[base + q].g - 1)));
+      }
+      bool free_slot = false;
+      for (int spin = 0; spin < (1 << 14) && !free_slot; ++spin) {
+        free_slot = ld_acquire(&P.seq[t & mask]) == t;
+        if (!free_slot) __nanosleep(64);
+      }
+      if (!free_slot) {
+        if (atomicCAS(&ctl->error, 0, SP_ERR_CAPACITY) == 0) ctl->err_info[0] = t;
+        continue;
+      }
+      Task *D = &P.tasks[t & mask];
+      D->sub = base + q;
+      D->plen = 0;
+      D->mask = 0xF;
+      D->flags = (uint8_t)kk;
+      st_release(&P.seq[t & mask], t + 1u);
+    }
+    __syncwarp();
+    return;
+  }
+}
+
+// Resident threads per SM the search kernels are compiled for (the register
+// budget: 768 threads leave 80 registers a thread; 24 warps per SM hide the
+// pattern-table latency markedly better than 16).
+#ifndef SP_SEARCH_THREADS_PER_SM
+#define SP_SEARCH_THREADS_PER_SM 768
+#endif
+
+template <int W, bool PDB, int BLOCK, int WORDS, bool MULTI>
+__global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) search_round_kernel(RoundParams P) {
   constexpr int N = W * W;
   constexpr int BSTRIDE = 28;  // bytes per lane board (7 words: conflict-free same-cell access)
   constexpr int MAXLEV = WORDS * 16;
@@ -118,6 +258,9 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
   __shared__ uint32_t s_stack[WORDS][BLOCK];
   __shared__ uint32_t s_prefix[kPathWords][BLOCK];  // the lane's task prefix (its pool slot is freed)
   __shared__ __align__(16) uint8_t s_board[W == 5 ? BLOCK * BSTRIDE : 4];
+  // multi-iteration mode: per-warp bucket counts of the longest-first publication
+  __shared__ uint32_t s_hist[MULTI ? BLOCK / 32 : 1][32];
+  __shared__ uint32_t s_cold[3][BLOCK];  // per-lane data of rare events (below)
   // block-wide cache of the pool state: at most one global poll per block per poll_ns
   __shared__ uint32_t s_pool[5];  // head, tail, error, outstanding, heartbeat
   __shared__ unsigned long long s_pool_t;
@@ -161,6 +304,17 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
   ir.clear();
   iff.clear();
   unsigned long long c_tries = 0, c_notfree = 0, c_nowait = 0, c_done = 0, c_found = 0;  // donation counters
+  uint32_t cur_inst = 0;  // the task's instance
+  int splitk = 0;         // split task: hand every node at this relative depth to the pool
+  bool emit_pending = false;
+  // Rare per-lane events, flags in a register and their data in shared memory:
+  //  * kAdvance: the lane finished an instance's iteration; the warp advances
+  //    that instance (s_cold[0]) at the top of its next loop;
+  //  * kDebt: a reserved pool index (s_cold[1]) whose ring slot did not free
+  //    in time is owed: the lane kept the work and publishes a null task (no
+  //    moves, SubRoot s_cold[2]) there later, so no index stays unpublished.
+  constexpr uint32_t kAdvance = 1u, kDebt = 2u;
+  uint32_t events = 0;
 
   auto tile_at = [&](int c) -> int {
     if (W == 4) return (int)((b64 >> (4 * c)) & 15u);
@@ -228,12 +382,40 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
   auto set_error = [&](int code, uint32_t info) {
     if (atomicCAS(&ctl->error, 0, code) == 0) ctl->err_info[0] = info;
   };
+  // Wait a bounded time for the ring slot of reserved pool index t (normally
+  // free at once: its previous occupant, index t - cap, was claimed long
+  // before).
+  auto slot_free = [&](uint32_t t, int spins) -> bool {
+    for (int spin = 0; spin < spins; ++spin) {
+      if (ld_acquire(&P.seq[t & (P.cap - 1u)]) == t) return true;
+      __nanosleep(64);
+    }
+    return false;
+  };
   auto finish_task = [&]() {
     ++c_done;
-    if (cnt) atomicAdd(&P.sub_nodes[sub], cnt);
+    state = 0;
+    if (MULTI) {
+      if (cnt) {
+        // the instance stays in the task's iteration while the task is outstanding
+        const int cur_iter = ld_volatile(&P.inst_iter[cur_inst]);
+        atomicAdd(&P.iter_nodes[(size_t)cur_inst * kMaxIters + cur_iter], cnt);
+        atomicAdd(&P.sub_loads[(size_t)(cur_iter & 1) * P.n_subs + sub], cnt);
+      }
+      __threadfence();
+      // the last task of the iteration: the warp advances the instance at the
+      // top of its next loop, and only then does this task leave
+      // `outstanding`, so that never reads 0 while work is still to come
+      if (atomicSub(&P.inst_out[cur_inst], 1u) == 1u) {
+        events |= kAdvance;
+        s_cold[0][tid] = cur_inst;
+        return;
+      }
+    } else if (cnt) {
+      atomicAdd(&P.sub_nodes[sub], cnt);
+    }
     __threadfence();
     atomicSub(&ctl->outstanding, 1u);
-    state = 0;
   };
   // Copy the claimed record out of its ring slot, then free the slot for the
   // producer of index slot + cap.
@@ -244,6 +426,7 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
     const uint32_t hdr = __ldcg((const uint32_t *)T + 1);
     plen = (int)(hdr & 0xFFFFu);
     mask0 = (hdr >> 16) & 0xFu;
+    splitk = (int)(hdr >> 24);
     for (int wi = 0; wi < kPathWords; ++wi) s_prefix[wi][tid] = __ldcg(&T->path[wi]);
     st_release(&P.seq[s], slot + P.cap);  // the copy above completes before the slot is reused
   };
@@ -264,7 +447,12 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
     g = tb[26 - 16];
     pre = tb[27 - 16] == kNoPre ? -1 : (int)tb[27 - 16];
     uint32_t inst = *(const uint32_t *)(tb + 12);
-    limit = P.inst_limit[inst];
+    cur_inst = inst;
+    if (MULTI) {
+      limit = ld_volatile(&P.inst_limit[inst]);
+    } else {
+      limit = P.inst_limit[inst];
+    }
     for (int i = 0; i < plen; ++i) {
       int d = task_dir(i);
       if (!((legal_moves(W, blank) >> d) & 1u)) {  // corrupt record: never index off the board
@@ -342,6 +530,13 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
         pre = d;
         it = 0;
         if (nh == 0) record_goal();
+        if (splitk && k == splitk) {
+          // split task: this node (already counted as generated) becomes a
+          // task of its own (published outside the step loop); the lane then
+          // steps back
+          emit_pending = true;
+          it = 4;
+        }
       } else {
         it = d + 1;
       }
@@ -410,6 +605,30 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
 
   for (;;) {
     const long long t_iter = clock64();
+    // pending work of the previous loop: instance advances, then owed indices
+    if (MULTI) {
+      unsigned pend = __ballot_sync(FULL, events & kAdvance);
+      while (pend) {
+        const int src = __ffs(pend) - 1;
+        pend &= pend - 1u;
+        warp_advance(P, s_cold[0][(tid & ~31) + src], s_hist[tid >> 5]);
+        if (lane == src) {
+          events &= ~kAdvance;
+          __threadfence();
+          atomicSub(&ctl->outstanding, 1u);
+        }
+      }
+    }
+    if ((events & kDebt) && ld_acquire(&P.seq[s_cold[1][tid] & (P.cap - 1u)]) == s_cold[1][tid]) {
+      const uint32_t debt = s_cold[1][tid];
+      Task *D = &P.tasks[debt & (P.cap - 1u)];
+      D->sub = s_cold[2][tid];
+      D->plen = 0;
+      D->mask = 0;  // no first move: the claimant finishes it at once
+      D->flags = 0;
+      st_release(&P.seq[debt & (P.cap - 1u)], debt + 1u);
+      events &= ~kDebt;
+    }
     // 0. pool state from the block's cached copy (one global poll per block
     //    per poll_ns; a stale copy only delays, never corrupts, decisions:
     //    outstanding == 0 is final, tail and head only grow)
@@ -482,13 +701,44 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
     // 4. search
     c_slots += 32ull * (unsigned long long)P.steps;
     if (state == 2) {
+      bool fin = false;
       for (int s = 0; s < P.steps; ++s) {
         ++c_steps;
         if (step()) {
-          finish_task();
+          fin = true;
           break;
         }
+        if (emit_pending) break;
       }
+      if (emit_pending) {
+        emit_pending = false;
+        // the split is advisory: with a debt outstanding or the ring half
+        // full, the lane searches the subtree itself
+        bool emitted = false;
+        if (!(events & kDebt) && (int32_t)(tl - hd) <= (int32_t)(P.cap >> 1)) {
+          atomicAdd(&ctl->outstanding, 1u);
+          if (MULTI) atomicAdd(&P.inst_out[cur_inst], 1u);  // the lane's own task keeps it >= 1
+          const uint32_t t = atomicAdd(&ctl->tail, 1u);
+          if (slot_free(t, 4096)) {
+            const int len = plen + k;
+            Task *D = &P.tasks[t & (P.cap - 1u)];
+            D->sub = sub;
+            D->plen = (uint16_t)len;
+            D->mask = 0xF;
+            D->flags = 0;
+            for (int wi = 0; wi < kPathWords; ++wi) D->path[wi] = path_word(wi, len);
+            st_release(&P.seq[t & (P.cap - 1u)], t + 1u);
+            emitted = true;
+          } else {
+            ++c_notfree;
+            events |= kDebt;
+            s_cold[1][tid] = t;
+            s_cold[2][tid] = sub;
+          }
+        }
+        if (!emitted) it = 0;
+      }
+      if (fin) finish_task();
     }
     // 5. donate while fewer than `reserve` tasks are queued (tail - head)
     if (P.donate && hd + P.reserve > tl) {
@@ -503,7 +753,7 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
       const unsigned allowed = min(8u, 1u + shortfall / P.spread);
       const unsigned cand = __ballot_sync(FULL, lev >= 0 && (unsigned)lev <= best + 1u);
       const unsigned rank = __popc(cand & ((1u << lane) - 1u));
-      const bool donor = ((cand >> lane) & 1u) && rank < allowed;
+      const bool donor = ((cand >> lane) & 1u) && rank < allowed && !(events & kDebt);
       const unsigned donors = __ballot_sync(FULL, donor);
       if (lane == 0) {
         ++c_nowait;  // hungry polls
@@ -519,22 +769,18 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
       if (donor) {
         // the reserved index's ring slot is free once the slot's previous
         // occupant (index t - cap, claimed long before) was copied out, which
-        // in practice it already is -- wait a bounded time, else leave the
-        // index unpublished (its claimant then idles until the round ends)
+        // in practice it already is -- wait a bounded time, else keep the
+        // branch and owe the index a null task
         const uint32_t mask = P.cap - 1u;
         ++c_tries;
+        if (MULTI) atomicAdd(&P.inst_out[cur_inst], 1u);  // the donor's own task keeps it >= 1
         const uint32_t t = tbase + (uint32_t)__popc(donors & ((1u << lane) - 1u));
-        bool ok = false;
-        for (int spin = 0; spin < 4096; ++spin) {
-          if (ld_acquire(&P.seq[t & mask]) == t) {
-            ok = true;
-            break;
-          }
-          __nanosleep(64);
-        }
+        const bool ok = slot_free(t, 4096);
         if (!ok) {
           ++c_notfree;
-          atomicSub(&ctl->outstanding, 1u);  // nothing published at t
+          events |= kDebt;
+          s_cold[1][tid] = t;
+          s_cold[2][tid] = sub;
         }
         if (ok) {
           Task *D = &P.tasks[t & mask];
@@ -542,7 +788,7 @@ __global__ void __launch_bounds__(BLOCK) search_round_kernel(RoundParams P) {
           D->sub = sub;
           D->plen = (uint16_t)nlen;
           D->mask = (uint8_t)dmask;
-          D->flags = 1;
+          D->flags = 0;
           for (int wi = 0; wi < kPathWords; ++wi) D->path[wi] = path_word(wi, nlen);
           st_release(&P.seq[t & mask], t + 1u);
           atomicAdd(&ctl->donated, 1ull);
@@ -701,11 +947,12 @@ cudaError_t launch_split_level(int w, bool pdb, int num_sms, const SplitArgs &A,
 }
 
 // Host launchers (template kernels stay in this translation unit).
-cudaError_t launch_search_round(int w, bool pdb, int block, int blocks_per_sm, int num_sms,
-                                const RoundParams &P, cudaStream_t st, int *grid_out) {
+template <bool MULTI>
+static cudaError_t launch_impl(int w, bool pdb, int block, int blocks_per_sm, int num_sms, const RoundParams &P,
+                               cudaStream_t st, int *grid_out) {
   void (*kern)(RoundParams) = nullptr;
 #define SP_PICK(W, PD, B, WD) \
-  if (w == W && pdb == PD && block == B) kern = search_round_kernel<W, PD, B, WD>;
+  if (w == W && pdb == PD && block == B) kern = search_round_kernel<W, PD, B, WD, MULTI>;
   SP_PICK(4, false, 256, 6)
   SP_PICK(4, true, 256, 6)
   SP_PICK(5, false, 256, 10)
@@ -727,6 +974,16 @@ cudaError_t launch_search_round(int w, bool pdb, int block, int blocks_per_sm, i
   kern<<<grid, block, 0, st>>>(P);
   note_launch();
   return cudaGetLastError();
+}
+
+cudaError_t launch_search_round(int w, bool pdb, int block, int blocks_per_sm, int num_sms,
+                                const RoundParams &P, cudaStream_t st, int *grid_out) {
+  return launch_impl<false>(w, pdb, block, blocks_per_sm, num_sms, P, st, grid_out);
+}
+
+cudaError_t launch_search_multi(int w, bool pdb, int block, int blocks_per_sm, int num_sms,
+                                const RoundParams &P, cudaStream_t st, int *grid_out) {
+  return launch_impl<true>(w, pdb, block, blocks_per_sm, num_sms, P, st, grid_out);
 }
 
 cudaError_t launch_pool_init(Task *tasks, const Task *emit, const uint32_t *n_emit, const uint32_t *direct,

@@ -117,6 +117,19 @@ struct Pinned {
   }
 };
 
+// Device tables of the multi-iteration mode (grow-only).
+struct MultiBufs {
+  int32_t *iter = nullptr, *fin = nullptr, *status = nullptr, *goal = nullptr, *subf = nullptr, *ifv = nullptr;
+  uint32_t *out = nullptr, *base = nullptr, *nsub = nullptr, *ioff = nullptr, *ilen = nullptr;
+  unsigned long long *icum = nullptr, *iter_nodes = nullptr, *loads = nullptr;
+  size_t cap_iter = 0, cap_fin = 0, cap_status = 0, cap_goal = 0, cap_subf = 0, cap_ifv = 0, cap_out = 0,
+         cap_base = 0, cap_nsub = 0, cap_ioff = 0, cap_ilen = 0, cap_icum = 0, cap_iter_nodes = 0, cap_loads = 0;
+  void release() {
+    void *ptrs[] = {iter, fin, status, goal, subf, ifv, out, base, nsub, ioff, ilen, icum, iter_nodes, loads};
+    for (void *p : ptrs) cudaFree(p);
+  }
+};
+
 }  // namespace
 }  // namespace sp
 
@@ -168,6 +181,7 @@ struct sp_solver {
   Pinned<uint8_t> h_boards;
   Pinned<int32_t> h_hv;
   Pinned<SubRoot> h_subs;
+  MultiBufs mb;
   std::string err;
   sp_stats stats{};
 };
@@ -435,7 +449,8 @@ void fold_ctl(sp_solver *s, const PoolCtl &ctl, int ri, float ms) {
 
 // Launch one round: uploads, split pre-pass, pool set-up, search; then the
 // control block, split counters, per-root counts and solutions come back.
-int launch_round(sp_solver *s, const RoundPlan &plan, size_t n_subs, size_t n_inst, float *ms) {
+int launch_round(sp_solver *s, const RoundPlan &plan, size_t n_subs, size_t n_inst, float *ms,
+                 bool multi = false) {
   const uint32_t n_direct = (uint32_t)plan.direct.size();
   int rc = ensure_pool(s, plan.direct.size() + plan.emit_bound);
   if (rc) return rc;
@@ -512,15 +527,37 @@ int launch_round(sp_solver *s, const RoundPlan &plan, size_t n_subs, size_t n_in
                                                                           : lanes / 16u;
   P.spread = std::max(1u, lanes / 32u);
   int grid = 0;
-  SP_CUDA(s, launch_search_round(s->w, s->heur == SP_HEUR_PDB, block, s->cfg.blocks_per_sm, s->num_sms, P,
-                                 s->st, &grid));
+  if (multi) {
+    MultiBufs &m = s->mb;
+    P.inst_iter = m.iter;
+    P.inst_out = m.out;
+    P.inst_final = m.fin;
+    P.inst_status = m.status;
+    P.inst_sub_base = m.base;
+    P.inst_nsub = m.nsub;
+    P.sub_maxf = m.subf;
+    P.inter_off = m.ioff;
+    P.inter_len = m.ilen;
+    P.inter_f = m.ifv;
+    P.inter_cum = m.icum;
+    P.goal_maxf = m.goal;
+    P.iter_nodes = m.iter_nodes;
+    P.sub_loads = m.loads;
+    P.n_subs = (uint32_t)n_subs;
+    P.static_split = s->cfg.lb_mode == SP_LB_STATIC_STEAL ? 1 : 0;
+    SP_CUDA(s, launch_search_multi(s->w, s->heur == SP_HEUR_PDB, block, s->cfg.blocks_per_sm, s->num_sms, P,
+                                   s->st, &grid));
+  } else {
+    SP_CUDA(s, launch_search_round(s->w, s->heur == SP_HEUR_PDB, block, s->cfg.blocks_per_sm, s->num_sms, P,
+                                   s->st, &grid));
+  }
   SP_CUDA(s, cudaEventRecord(s->ev1, s->st));
   SP_CUDA(s, s->h_ctl.reserve(1));
   SP_CUDA(s, s->h_sub_nodes.reserve(std::max<size_t>(n_subs, 1)));
   SP_CUDA(s, s->h_sols.reserve(std::max<size_t>(n_inst, 1)));
   SP_CUDA(s, cudaMemcpyAsync(s->h_ctl.p, s->d_ctl, sizeof(PoolCtl), cudaMemcpyDeviceToHost, s->st));
   SP_CUDA(s, cudaMemcpyAsync(s->h_cnt.p, s->d_cnt, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s->st));
-  if (n_subs)
+  if (n_subs && !multi)
     SP_CUDA(s, cudaMemcpyAsync(s->h_sub_nodes.p, s->d_sub_nodes, n_subs * sizeof(unsigned long long),
                                cudaMemcpyDeviceToHost, s->st));
   if (n_inst)
@@ -628,6 +665,204 @@ void plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int
   for (int l = 1; l < 12; ++l) plan.level_bound = std::max(plan.level_bound, level[l]);
 }
 
+// Result path of a solved instance: the root-set tree prefix to its goal (a
+// tree node) or to the device solution's root, then the device's moves.
+void set_path(int w, Instance &I, const uint8_t *tiles, int host_goal, const Solution *sol) {
+  std::vector<uint8_t> mv;
+  int node = host_goal;
+  uint32_t extra = 0;
+  const uint32_t *pw = nullptr;
+  if (node < 0) {
+    node = I.leaves[sol->sub - I.sub_base];
+    extra = sol->len;
+    pw = sol->path;
+  }
+  for (int x = node; x > 0; x = I.tree[(size_t)x].parent) mv.push_back(I.tree[(size_t)x].move);
+  std::reverse(mv.begin(), mv.end());
+  for (uint32_t j = 0; j < extra; ++j) mv.push_back((uint8_t)((pw[j >> 4] >> (2 * (j & 15))) & 3u));
+  sp_result *R = I.out;
+  R->len = (int32_t)mv.size();
+  if (mv.size() > SP_MAX_MOVES) {
+    R->status = SP_ERR_PATH;
+  } else {
+    R->n_moves = R->len;
+    memcpy(R->moves, mv.data(), mv.size());
+    R->status = replay_ok(w, tiles, R->moves, R->n_moves) ? SP_OK : SP_ERR_PATH;
+  }
+}
+
+int tree_goal(const Instance &I, int L) {
+  int best = -1;
+  for (int32_t x : I.goals) {
+    const TreeNode &t = I.tree[(size_t)x];
+    if (t.maxf <= L && (best < 0 || t.g < I.tree[(size_t)best].g)) best = x;
+  }
+  return best;
+}
+
+// Multi-iteration mode: every instance's threshold loop runs on the device in
+// one launch (search.cu, `advance`); the host only prepares the tables and
+// assembles the results.  Iterations in which no root-set leaf is active are
+// finished here first.
+int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst, size_t n_subs,
+                std::chrono::steady_clock::time_point t_start) {
+  const size_t ni = inst.size();
+  const int w = s->w, n = s->n;
+  std::vector<int32_t> h_iter(ni, 0), h_limit(ni, 0), h_final(ni, -1), h_goal(ni, 0x7FFFFFFF);
+  std::vector<uint32_t> h_out(ni, 0), h_base(ni, 0), h_nsub(ni, 0), h_ioff(ni, 0), h_ilen(ni, 0);
+  std::vector<int32_t> h_subf(std::max<size_t>(n_subs, 1), 0x7FFFFFFF), h_if;
+  std::vector<unsigned long long> h_icum;
+  std::vector<uint32_t> direct;
+  for (size_t i = 0; i < ni; ++i) {
+    Instance &I = inst[i];
+    h_base[i] = I.sub_base;
+    if (I.done) continue;
+    for (int32_t x : I.goals) h_goal[i] = std::min(h_goal[i], I.tree[(size_t)x].maxf);
+    h_ioff[i] = (uint32_t)h_if.size();
+    h_ilen[i] = (uint32_t)I.interior.size();
+    for (auto &e : I.interior) {
+      h_if.push_back(e.first);
+      h_icum.push_back(e.second);
+    }
+    for (size_t q = 0; q < I.leaves.size(); ++q) h_subf[I.sub_base + q] = I.leaf_maxf[q];
+    h_nsub[i] = (uint32_t)I.leaves.size();
+    // iterations without any active leaf: the root-set tree holds them whole
+    int L = I.h0;
+    for (;;) {
+      const size_t na = active_leaves(I, L);
+      if (na) {
+        for (size_t q = 0; q < na; ++q) direct.push_back(I.sub_base + (uint32_t)q);
+        h_out[i] = (uint32_t)na;
+        h_iter[i] = I.iter;
+        h_limit[i] = L;
+        break;
+      }
+      sp_result *R = I.out;
+      R->f_limit[I.iter] = L;
+      R->nodes[I.iter] = interior_nodes(I, L);
+      R->nodes_total += R->nodes[I.iter];
+      R->n_iter = I.iter + 1;
+      const int hg = tree_goal(I, L);
+      if (hg >= 0) {
+        set_path(w, I, tiles + i * (size_t)n, hg, nullptr);
+        I.done = true;
+        break;
+      }
+      if (++I.iter >= SP_MAX_ITERS) {
+        R->status = SP_ERR_LIMIT;
+        I.done = true;
+        break;
+      }
+      L += 2;
+    }
+    if (I.done) h_nsub[i] = 0;
+  }
+  if (h_if.empty()) {
+    h_if.push_back(0);
+    h_icum.push_back(0);
+  }
+  MultiBufs &m = s->mb;
+  int rc = 0;
+  if ((rc = ensure(s, &m.iter, &m.cap_iter, ni)) || (rc = ensure(s, &m.out, &m.cap_out, ni)) ||
+      (rc = ensure(s, &m.fin, &m.cap_fin, ni)) || (rc = ensure(s, &m.status, &m.cap_status, ni)) ||
+      (rc = ensure(s, &m.base, &m.cap_base, ni)) || (rc = ensure(s, &m.nsub, &m.cap_nsub, ni)) ||
+      (rc = ensure(s, &m.ioff, &m.cap_ioff, ni)) || (rc = ensure(s, &m.ilen, &m.cap_ilen, ni)) ||
+      (rc = ensure(s, &m.goal, &m.cap_goal, ni)) || (rc = ensure(s, &m.subf, &m.cap_subf, h_subf.size())) ||
+      (rc = ensure(s, &m.ifv, &m.cap_ifv, h_if.size())) || (rc = ensure(s, &m.icum, &m.cap_icum, h_icum.size())) ||
+      (rc = ensure(s, &m.iter_nodes, &m.cap_iter_nodes, ni * kMaxIters)) ||
+      (rc = ensure(s, &m.loads, &m.cap_loads, 2 * std::max<size_t>(n_subs, 1))))
+    return rc;
+  auto up = [&](auto *dst, const auto &v) {
+    return cudaMemcpyAsync(dst, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice, s->st);
+  };
+  SP_CUDA(s, up(m.iter, h_iter));
+  SP_CUDA(s, up(s->d_limit, h_limit));
+  SP_CUDA(s, up(m.out, h_out));
+  SP_CUDA(s, up(m.fin, h_final));
+  SP_CUDA(s, cudaMemsetAsync(m.status, 0, ni * sizeof(int32_t), s->st));
+  SP_CUDA(s, up(m.base, h_base));
+  SP_CUDA(s, up(m.nsub, h_nsub));
+  SP_CUDA(s, up(m.ioff, h_ioff));
+  SP_CUDA(s, up(m.ilen, h_ilen));
+  SP_CUDA(s, up(m.goal, h_goal));
+  SP_CUDA(s, up(m.subf, h_subf));
+  SP_CUDA(s, up(m.ifv, h_if));
+  SP_CUDA(s, up(m.icum, h_icum));
+  SP_CUDA(s, cudaMemsetAsync(m.iter_nodes, 0, ni * kMaxIters * sizeof(unsigned long long), s->st));
+  SP_CUDA(s, cudaMemsetAsync(m.loads, 0, 2 * std::max<size_t>(n_subs, 1) * sizeof(unsigned long long), s->st));
+  SP_CUDA(s, cudaMemsetAsync(s->d_sol, 0, ni * sizeof(Solution), s->st));
+  s->stats.h2d_bytes += ni * 40 + h_subf.size() * 4 + h_if.size() * 12;
+  float ms = 0;
+  if (!direct.empty()) {
+    RoundPlan plan;
+    plan.direct = std::move(direct);
+    // later iterations publish up to every root at once, and split pieces
+    // while the ring is below half full
+    plan.emit_bound = n_subs + ((size_t)1 << 20);
+    rc = launch_round(s, plan, n_subs, ni, &ms, true);
+    if (rc) return rc;
+    const PoolCtl &ctl = *s->h_ctl.p;
+    fold_ctl(s, ctl, 0, ms);
+    s->stats.tasks_initial += plan.direct.size();
+    s->stats.round_tasks[0] = (int32_t)plan.direct.size();
+    if (ctl.error) {
+      char buf[160];
+      snprintf(buf, sizeof buf, "device error %d (info %u) in the multi-iteration search", ctl.error,
+               ctl.err_info[0]);
+      s->err = buf;
+      for (auto &I : inst)
+        if (!I.done) {
+          I.out->status = ctl.error;
+          I.done = true;
+        }
+      return ctl.error;
+    }
+  }
+  std::vector<int32_t> fin(ni), st(ni);
+  std::vector<unsigned long long> itn(ni * kMaxIters);
+  SP_CUDA(s, cudaMemcpyAsync(fin.data(), m.fin, ni * sizeof(int32_t), cudaMemcpyDeviceToHost, s->st));
+  SP_CUDA(s, cudaMemcpyAsync(st.data(), m.status, ni * sizeof(int32_t), cudaMemcpyDeviceToHost, s->st));
+  SP_CUDA(s, cudaMemcpyAsync(itn.data(), m.iter_nodes, itn.size() * sizeof(unsigned long long),
+                             cudaMemcpyDeviceToHost, s->st));
+  SP_CUDA(s, cudaStreamSynchronize(s->st));
+  s->stats.d2h_bytes += ni * (8 + kMaxIters * 8);
+  const Solution *sols = s->h_sols.p;
+  int rounds = 0;
+  for (size_t i = 0; i < ni; ++i) {
+    Instance &I = inst[i];
+    if (I.done) {
+      rounds = std::max(rounds, I.out->n_iter);
+      continue;
+    }
+    sp_result *R = I.out;
+    const int r_end = fin[i] < 0 ? I.iter : fin[i];
+    for (int r = I.iter; r <= r_end && r < SP_MAX_ITERS; ++r) {
+      R->f_limit[r] = I.h0 + 2 * r;
+      R->nodes[r] = itn[i * kMaxIters + (size_t)r];
+      R->nodes_total += R->nodes[r];
+      s->stats.nodes += R->nodes[r];
+      s->stats.round_nodes[std::min(r, SP_MAX_ROUNDS - 1)] += R->nodes[r];
+    }
+    R->n_iter = r_end + 1;
+    rounds = std::max(rounds, R->n_iter);
+    if (fin[i] < 0) {
+      R->status = SP_ERR_TIMEOUT;
+    } else if (st[i]) {
+      R->status = st[i];
+    } else {
+      const int L = I.h0 + 2 * fin[i];
+      const int hg = tree_goal(I, L);
+      set_path(w, I, tiles + i * (size_t)n, hg, hg < 0 ? &sols[i] : nullptr);
+    }
+    I.done = true;
+  }
+  s->stats.rounds = rounds;
+  const double wall = ms_since(t_start);
+  for (auto &I : inst) I.out->seconds = wall / 1000.0;
+  s->stats.wall_ms = wall;
+  return SP_OK;
+}
+
 int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
   auto t_start = std::chrono::steady_clock::now();
   memset(&s->stats, 0, sizeof(s->stats));
@@ -717,6 +952,7 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
   }
   SP_CUDA(s, s->h_limits.reserve(inst.size()));
   s->stats.frontier_ms += ms_since(t_front);
+  if (s->cfg.persistent) return solve_multi(s, tiles, inst, n_subs, t_start);
 
   std::vector<int32_t> limits(inst.size(), 0);
   for (int round = 0; round < SP_MAX_ITERS; ++round) {
@@ -837,7 +1073,8 @@ bool config_ok(const sp_config *c) {
          c->frontier_target <= (1 << 20) && c->blocks_per_sm >= 0 && c->blocks_per_sm <= 16 &&
          c->lb_mode >= SP_LB_STEAL && c->lb_mode <= SP_LB_NONE && c->donate_min_slack >= 0 &&
          c->steps_per_poll >= 1 && c->steps_per_poll <= 4096 && c->timeout_ms >= 100 &&
-         c->timeout_ms <= 600000 && c->static_split_cap >= 1 && c->donate_reserve >= -1;
+         c->timeout_ms <= 600000 && c->static_split_cap >= 1 && c->donate_reserve >= -1 &&
+         (c->persistent == 0 || c->persistent == 1);
 }
 
 }  // namespace
@@ -855,6 +1092,7 @@ void sp_config_default(sp_config *c) {
   c->timeout_ms = 20000;
   c->static_split_cap = 10;
   c->donate_reserve = 0;
+  c->persistent = 0;
 }
 
 int sp_create(int width, int heuristic, const sp_config *cfg, sp_solver **out) {
@@ -912,6 +1150,7 @@ void sp_destroy(sp_solver *s) {
   cudaFree(s->d_split_a);
   cudaFree(s->d_split_b);
   cudaFree(s->d_emit);
+  s->mb.release();
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->st) cudaStreamDestroy(s->st);

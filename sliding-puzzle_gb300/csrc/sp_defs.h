@@ -12,6 +12,7 @@
 namespace sp {
 
 constexpr int kMaxN = 25;
+constexpr int kMaxIters = 96;                // threshold iterations per instance
 constexpr int kPathWords = 10;               // 2-bit moves: 160 moves per record
 constexpr int kMaxPath = kPathWords * 16;
 constexpr uint8_t kNoPre = 0xFF;

@@ -30,10 +30,30 @@ struct RoundParams {
   uint32_t pad1;
   unsigned long long timeout_ns;
   unsigned long long poll_ns;  // min interval of a block's global pool poll
+  // multi-iteration mode: every instance runs its own threshold loop on the
+  // device (inst_limit is then written by the kernel as well)
+  int32_t *inst_iter;                 // current iteration
+  uint32_t *inst_out;                 // tasks of the current iteration not finished
+  int32_t *inst_final;                // iteration that ended the search, -1 while running
+  int32_t *inst_status;
+  const uint32_t *inst_sub_base;      // the instance's roots: subs[base .. base+nsub),
+  const uint32_t *inst_nsub;          //   sorted by sub_maxf
+  const int32_t *sub_maxf;            // prefix max of g+h along the root's path
+  const uint32_t *inter_off, *inter_len;  // per instance: (f, cumulative children) pairs
+  const int32_t *inter_f;             //   of root-set interior nodes, sorted by f
+  const unsigned long long *inter_cum;
+  const int32_t *goal_maxf;           // smallest maxf of a root-set goal node (INT32_MAX: none)
+  unsigned long long *iter_nodes;     // [instance][kMaxIters] generated nodes
+  unsigned long long *sub_loads;      // [2][n_subs] per-root loads of the last two iterations
+  uint32_t n_subs;
+  int32_t static_split;
 };
 
 // One threshold round: grid = num_sms * blocks_per_sm (0 = occupancy maximum).
 cudaError_t launch_search_round(int w, bool pdb, int block, int blocks_per_sm, int num_sms,
+                                const RoundParams &P, cudaStream_t st, int *grid_out);
+// The whole threshold loop of a batch in one launch (multi-iteration mode).
+cudaError_t launch_search_multi(int w, bool pdb, int block, int blocks_per_sm, int num_sms,
                                 const RoundParams &P, cudaStream_t st, int *grid_out);
 // Publish the round's tasks (split pieces first, then the direct tasks) and
 // reset the pool control block.

@@ -33,7 +33,7 @@ class SpConfig(ctypes.Structure):
                 ("blocks_per_sm", ctypes.c_int32), ("lb_mode", ctypes.c_int32),
                 ("donate_min_slack", ctypes.c_int32), ("steps_per_poll", ctypes.c_int32),
                 ("timeout_ms", ctypes.c_int32), ("static_split_cap", ctypes.c_int32),
-                ("donate_reserve", ctypes.c_int32)]
+                ("donate_reserve", ctypes.c_int32), ("persistent", ctypes.c_int32)]
 
 
 class SpResult(ctypes.Structure):
