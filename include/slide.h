@@ -64,7 +64,9 @@ typedef enum {
   SP_LB_STATIC_STEAL = 1,  /* + reference-style static re-split from the
                               previous round's loads
                               (src/24puzzle_block_parallel_with_pdb.cu:839-897) */
-  SP_LB_NONE = 2           /* root set only: no re-split, no donation */
+  SP_LB_NONE = 2,          /* root set only: no re-split, no donation */
+  SP_LB_LEARNED = 3        /* SP_LB_STATIC_STEAL, with roots that have no measured
+                              load predicted by the learned model (sp_lbm_*) */
 } sp_lb_mode;
 
 typedef struct {
@@ -193,6 +195,31 @@ int sp_dfs_round(sp_solver *s, const uint8_t *roots, const int32_t *depth,
 int sp_dfs_round_md_noalloc(int width, const uint8_t *d_roots, const int32_t *d_depth,
                             const int32_t *d_pre, int n, int limit, uint64_t *d_nodes,
                             int32_t *d_found, void *stream);
+
+/* Learned load balancer (no reference counterpart; the reference balances
+ * only from the previous round's measured loads,
+ * src/24puzzle_block_parallel_with_pdb.cu:839-897).  An MLP
+ * ((N-1)*N one-hot tile placement + slack -> 256 -> 256 -> 1, ReLU, BF16
+ * weights and activations, FP32 accumulation, tcgen05 tensor cores) predicts
+ * log2(1 + generated nodes) of a root's subtree at threshold
+ * f(root) + 2*slack.  The model belongs to the solver. */
+uint64_t sp_lbm_num_params(int width);  /* floats: W1[D][256] b1 W2[256][256] b2 w3 b3, D = (N-1)*N+1 */
+int sp_lbm_init(sp_solver *s, uint64_t seed);                  /* He-normal, seeded */
+int sp_lbm_import(sp_solver *s, const float *src, uint64_t n);
+int sp_lbm_export(sp_solver *s, float *dst, uint64_t n);
+/* out[i] = predicted log2(1 + nodes) for tiles i (n*N bytes) at slack[i]. */
+int sp_lbm_predict(sp_solver *s, const uint8_t *tiles, const int32_t *slack, int n, float *out);
+/* One Adam step (lr) on the mean squared error against target[i] =
+ * log2(1 + nodes); n a multiple of 128.  loss may be NULL. */
+int sp_lbm_train_step(sp_solver *s, const uint8_t *tiles, const int32_t *slack, const float *target, int n,
+                      float lr, float *loss);
+/* The gradient of that loss (sp_lbm_num_params floats) without a step. */
+int sp_lbm_gradients(sp_solver *s, const uint8_t *tiles, const int32_t *slack, const float *target, int n,
+                     float *grads, float *loss);
+/* c[m][256] = a[m][k] . b[256][k]^T on the tensor cores (bf16 bit patterns
+ * in, fp32 out, host arrays; m a multiple of 128, n = 256, k a multiple of
+ * 64): the model's GEMM on its own, for testing. */
+int sp_gemm_bf16_nt(const uint16_t *a, const uint16_t *b, float *c, int m, int n, int k);
 
 int sp_last_stats(const sp_solver *s, sp_stats *out);
 const char *sp_status_string(int status);

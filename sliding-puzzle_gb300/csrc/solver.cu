@@ -35,6 +35,7 @@
 #include <vector>
 
 #include "../../include/slide.h"
+#include "lbm.h"
 #include "sp_defs.h"
 #include "sp_kernels.h"
 
@@ -182,6 +183,7 @@ struct sp_solver {
   Pinned<int32_t> h_hv;
   Pinned<SubRoot> h_subs;
   MultiBufs mb;
+  std::unique_ptr<lbm::Model> lbm;  // learned load balancer (SP_LB_LEARNED)
   std::string err;
   sp_stats stats{};
 };
@@ -544,7 +546,7 @@ int launch_round(sp_solver *s, const RoundPlan &plan, size_t n_subs, size_t n_in
     P.iter_nodes = m.iter_nodes;
     P.sub_loads = m.loads;
     P.n_subs = (uint32_t)n_subs;
-    P.static_split = s->cfg.lb_mode == SP_LB_STATIC_STEAL ? 1 : 0;
+    P.static_split = (s->cfg.lb_mode == SP_LB_STATIC_STEAL || s->cfg.lb_mode == SP_LB_LEARNED) ? 1 : 0;
     SP_CUDA(s, launch_search_multi(s->w, s->heur == SP_HEUR_PDB, block, s->cfg.blocks_per_sm, s->num_sms, P,
                                    s->st, &grid));
   } else {
@@ -577,16 +579,21 @@ int launch_round(sp_solver *s, const RoundPlan &plan, size_t n_subs, size_t n_in
 // predicted above the round's piece size T is split ceil(log2(pred/T))
 // levels by the device pre-pass -- the reference splits a root into
 // ceil(load/avg) pieces (src/24puzzle_block_parallel_with_pdb.cu:839-897) --
-// and whole roots are published in decreasing predicted size.
-void plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int32_t> &limits,
-                RoundPlan &plan) {
-  const bool stat = s->cfg.lb_mode == SP_LB_STATIC_STEAL;
+// and whole roots are published in decreasing predicted size.  With the
+// learned balancer, a root that has no measured load (not active in the
+// previous round) is predicted by the model instead of counting as 0.
+int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int32_t> &limits,
+               RoundPlan &plan) {
+  const bool learned = s->cfg.lb_mode == SP_LB_LEARNED;
+  const bool stat = s->cfg.lb_mode == SP_LB_STATIC_STEAL || learned;
   struct Cand {
     double pred;
     uint32_t sub;
     int room;  // levels left below the root before the limit
   };
   std::vector<Cand> c;
+  std::vector<uint32_t> q_sub, q_pos;  // roots for the model
+  std::vector<int32_t> q_slack;
   double total = 0;
   for (size_t i = 0; i < inst.size(); ++i) {
     Instance &I = inst[i];
@@ -600,12 +607,30 @@ void plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int
     if (I.prev_total > 0 && I.last_total > 0)
       growth = std::min(30.0, std::max(2.0, (double)I.last_total / (double)I.prev_total));
     for (size_t q = 0; q < na; ++q) {
+      const TreeNode &t = I.tree[(size_t)I.leaves[q]];
       const double p = (double)I.last_load[q] * growth;
-      c.push_back({p, I.sub_base + (uint32_t)q, limits[i] - (int)I.tree[(size_t)I.leaves[q]].g});
+      if (learned && I.last_load[q] == 0) {
+        q_sub.push_back(I.sub_base + (uint32_t)q);
+        q_pos.push_back((uint32_t)c.size());
+        q_slack.push_back(std::max(0, (limits[i] - (int)t.g - t.h) / 2));
+      }
+      c.push_back({p, I.sub_base + (uint32_t)q, limits[i] - (int)t.g});
       total += p;
     }
   }
-  if (!stat) return;
+  if (!stat) return SP_OK;
+  if (!q_sub.empty()) {
+    std::vector<float> y(q_sub.size());
+    int rc = s->lbm->predict_subs(s->d_subs, q_sub.data(), q_slack.data(), (int)q_sub.size(), y.data(), s->st,
+                                  s->err);
+    if (rc) return rc;
+    s->stats.kernel_launches += 2 * (int)((q_sub.size() + 65535) / 65536);
+    for (size_t k = 0; k < q_sub.size(); ++k) {
+      const double p = std::exp2(std::min(60.0, std::max(0.0, (double)y[k]))) - 1.0;
+      c[q_pos[k]].pred = p;
+      total += p;
+    }
+  }
   const double lanes = s->last_lanes > 0 ? (double)s->last_lanes : (double)s->num_sms * 1024.0;
   const double T = total / (lanes * 4.0);
   static const size_t pow3[12] = {1, 3, 9, 27, 81, 243, 729, 2187, 6561, 19683, 59049, 177147};
@@ -663,6 +688,7 @@ void plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int
     }
   }
   for (int l = 1; l < 12; ++l) plan.level_bound = std::max(plan.level_bound, level[l]);
+  return SP_OK;
 }
 
 // Result path of a solved instance: the root-set tree prefix to its goal (a
@@ -870,6 +896,10 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
     s->err = "PDB heuristic selected but sp_pdb_build/sp_pdb_import not done";
     return SP_ERR_NO_PDB;
   }
+  if (s->cfg.lb_mode == SP_LB_LEARNED && !(s->lbm && s->lbm->ready())) {
+    s->err = "learned load balancing selected but no model (sp_lbm_init/sp_lbm_import)";
+    return SP_ERR_ARG;
+  }
   const int w = s->w, n = s->n;
   std::vector<Instance> inst((size_t)nin);
   for (int i = 0; i < nin; ++i) {
@@ -967,7 +997,8 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
       s->h_limits.p[i] = limits[i];
     }
     RoundPlan plan;
-    plan_round(s, inst, limits, plan);
+    rc = plan_round(s, inst, limits, plan);
+    if (rc) return rc;
     SP_CUDA(s, cudaMemcpyAsync(s->d_limit, s->h_limits.p, inst.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
                                s->st));
     SP_CUDA(s, cudaMemsetAsync(s->d_sol, 0, inst.size() * sizeof(Solution), s->st));
@@ -1071,7 +1102,7 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
 bool config_ok(const sp_config *c) {
   return (c->threads_per_block == 128 || c->threads_per_block == 256) && c->frontier_target >= 1 &&
          c->frontier_target <= (1 << 20) && c->blocks_per_sm >= 0 && c->blocks_per_sm <= 16 &&
-         c->lb_mode >= SP_LB_STEAL && c->lb_mode <= SP_LB_NONE && c->donate_min_slack >= 0 &&
+         c->lb_mode >= SP_LB_STEAL && c->lb_mode <= SP_LB_LEARNED && c->donate_min_slack >= 0 &&
          c->steps_per_poll >= 1 && c->steps_per_poll <= 4096 && c->timeout_ms >= 100 &&
          c->timeout_ms <= 600000 && c->static_split_cap >= 1 && c->donate_reserve >= -1 &&
          (c->persistent == 0 || c->persistent == 1);
@@ -1332,6 +1363,89 @@ int sp_dfs_round(sp_solver *s, const uint8_t *roots, const int32_t *depth, const
   }
   for (int i = 0; i < n; ++i) s->stats.nodes += nodes[i];
   return SP_OK;
+}
+
+uint64_t sp_lbm_num_params(int width) {
+  return (width == 4 || width == 5) ? (uint64_t)lbm::num_params(width) : 0;
+}
+
+static int lbm_model(sp_solver *s, bool need_ready) {
+  if (!s) return SP_ERR_ARG;
+  if (!s->lbm) s->lbm.reset(new lbm::Model(s->w));
+  if (need_ready && !s->lbm->ready()) {
+    s->err = "no model: call sp_lbm_init or sp_lbm_import first";
+    return SP_ERR_ARG;
+  }
+  return SP_OK;
+}
+
+int sp_lbm_init(sp_solver *s, uint64_t seed) {
+  int rc = lbm_model(s, false);
+  return rc ? rc : s->lbm->init(seed, s->st, s->err);
+}
+
+int sp_lbm_import(sp_solver *s, const float *src, uint64_t n) {
+  if (!src) return SP_ERR_ARG;
+  int rc = lbm_model(s, false);
+  return rc ? rc : s->lbm->import_params(src, (size_t)n, s->st, s->err);
+}
+
+int sp_lbm_export(sp_solver *s, float *dst, uint64_t n) {
+  if (!dst) return SP_ERR_ARG;
+  int rc = lbm_model(s, true);
+  return rc ? rc : s->lbm->export_params(dst, (size_t)n, s->st, s->err);
+}
+
+static int lbm_check_rows(sp_solver *s, const uint8_t *tiles, const int32_t *slack, int n) {
+  if (!tiles || !slack || n < 0) return SP_ERR_ARG;
+  for (int i = 0; i < n; ++i) {
+    if (slack[i] < 0 || slack[i] > 255) {
+      s->err = "slack must lie in 0..255";
+      return SP_ERR_ARG;
+    }
+    uint32_t seen = 0;
+    for (int c = 0; c < s->n; ++c) {
+      const uint8_t t = tiles[(size_t)i * s->n + c];
+      if (t >= s->n || ((seen >> t) & 1u)) {
+        s->err = "tiles are not a permutation";
+        return SP_ERR_NOT_PERMUTATION;
+      }
+      seen |= 1u << t;
+    }
+  }
+  return SP_OK;
+}
+
+int sp_lbm_predict(sp_solver *s, const uint8_t *tiles, const int32_t *slack, int n, float *out) {
+  int rc = lbm_model(s, true);
+  if (!rc) rc = lbm_check_rows(s, tiles, slack, n);
+  if (rc) return rc;
+  if (!out) return SP_ERR_ARG;
+  return n ? s->lbm->predict(tiles, slack, n, out, s->st, s->err) : SP_OK;
+}
+
+int sp_lbm_train_step(sp_solver *s, const uint8_t *tiles, const int32_t *slack, const float *target, int n,
+                      float lr, float *loss) {
+  int rc = lbm_model(s, true);
+  if (!rc) rc = lbm_check_rows(s, tiles, slack, n);
+  if (rc) return rc;
+  if (!target || !(lr > 0.f)) return SP_ERR_ARG;
+  return s->lbm->train_step(tiles, slack, target, n, lr, true, loss, nullptr, s->st, s->err);
+}
+
+int sp_lbm_gradients(sp_solver *s, const uint8_t *tiles, const int32_t *slack, const float *target, int n,
+                     float *grads, float *loss) {
+  int rc = lbm_model(s, true);
+  if (!rc) rc = lbm_check_rows(s, tiles, slack, n);
+  if (rc) return rc;
+  if (!target || !grads) return SP_ERR_ARG;
+  return s->lbm->train_step(tiles, slack, target, n, 0.f, false, loss, grads, s->st, s->err);
+}
+
+int sp_gemm_bf16_nt(const uint16_t *a, const uint16_t *b, float *c, int m, int n, int k) {
+  if (!a || !b || !c) return SP_ERR_ARG;
+  std::string err;
+  return lbm::Model::gemm_nt(a, b, c, m, n, k, nullptr, err);
 }
 
 int sp_last_stats(const sp_solver *s, sp_stats *out) {

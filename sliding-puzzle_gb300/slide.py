@@ -18,7 +18,7 @@ LIB_PATH = os.path.join(HERE, "libslide.so")
 SP_MAX_ITERS = 96
 SP_MAX_MOVES = 240
 HEUR = {"manhattan": 0, "md": 0, "pdb": 1}
-LB = {"steal": 0, "static": 1, "static_steal": 1, "none": 2}
+LB = {"steal": 0, "static": 1, "static_steal": 1, "none": 2, "learned": 3}
 MOVE_NAMES = "URLD"  # blank moves: 0 up, 1 right, 2 left, 3 down
 
 
@@ -97,6 +97,14 @@ def load(build=True):
         "sp_status_string": (ctypes.c_char_p, [I32]),
         "sp_last_error": (ctypes.c_char_p, [P]),
         "sp_kernel_launch_count": (U64, []),
+        "sp_lbm_num_params": (U64, [I32]),
+        "sp_lbm_init": (I32, [P, U64]),
+        "sp_lbm_import": (I32, [P, P, U64]),
+        "sp_lbm_export": (I32, [P, P, U64]),
+        "sp_lbm_predict": (I32, [P, P, P, I32, P]),
+        "sp_lbm_train_step": (I32, [P, P, P, P, I32, ctypes.c_float, P]),
+        "sp_lbm_gradients": (I32, [P, P, P, P, I32, P, P]),
+        "sp_gemm_bf16_nt": (I32, [P, P, P, I32, I32, I32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -226,6 +234,51 @@ class Solver:
                                           nodes.ctypes.data, ctypes.byref(found)), "sp_dfs_round")
         return nodes, int(found.value)
 
+    # --- learned load balancer ---
+    def lbm_num_params(self):
+        return int(self.lib.sp_lbm_num_params(self.width))
+
+    def lbm_init(self, seed=1):
+        self._check(self.lib.sp_lbm_init(self.h, int(seed)), "sp_lbm_init")
+
+    def lbm_import(self, params):
+        a = np.ascontiguousarray(np.asarray(params, dtype=np.float32))
+        self._check(self.lib.sp_lbm_import(self.h, a.ctypes.data, a.size), "sp_lbm_import")
+
+    def lbm_export(self):
+        out = np.empty(self.lbm_num_params(), dtype=np.float32)
+        self._check(self.lib.sp_lbm_export(self.h, out.ctypes.data, out.size), "sp_lbm_export")
+        return out
+
+    def _lbm_rows(self, tiles, slack):
+        a = _as_tiles(tiles, self.width)
+        s = np.ascontiguousarray(np.asarray(slack, dtype=np.int32).reshape(a.shape[0]))
+        return a, s
+
+    def lbm_predict(self, tiles, slack):
+        a, s = self._lbm_rows(tiles, slack)
+        out = np.empty(a.shape[0], dtype=np.float32)
+        self._check(self.lib.sp_lbm_predict(self.h, a.ctypes.data, s.ctypes.data, a.shape[0], out.ctypes.data),
+                    "sp_lbm_predict")
+        return out
+
+    def lbm_train_step(self, tiles, slack, target, lr):
+        a, s = self._lbm_rows(tiles, slack)
+        t = np.ascontiguousarray(np.asarray(target, dtype=np.float32).reshape(a.shape[0]))
+        loss = ctypes.c_float(0)
+        self._check(self.lib.sp_lbm_train_step(self.h, a.ctypes.data, s.ctypes.data, t.ctypes.data, a.shape[0],
+                                               float(lr), ctypes.byref(loss)), "sp_lbm_train_step")
+        return float(loss.value)
+
+    def lbm_gradients(self, tiles, slack, target):
+        a, s = self._lbm_rows(tiles, slack)
+        t = np.ascontiguousarray(np.asarray(target, dtype=np.float32).reshape(a.shape[0]))
+        g = np.empty(self.lbm_num_params(), dtype=np.float32)
+        loss = ctypes.c_float(0)
+        self._check(self.lib.sp_lbm_gradients(self.h, a.ctypes.data, s.ctypes.data, t.ctypes.data, a.shape[0],
+                                              g.ctypes.data, ctypes.byref(loss)), "sp_lbm_gradients")
+        return float(loss.value), g
+
     def stats(self):
         s = SpStats()
         self._check(self.lib.sp_last_stats(self.h, ctypes.byref(s)), "sp_last_stats")
@@ -248,6 +301,20 @@ def result_dict(r):
         "moves": bytes(r.moves[: r.n_moves]),
         "seconds": float(r.seconds),
     }
+
+
+def gemm_bf16_nt(a_bits, b_bits):
+    """C = A . B^T on the tensor cores; A [m][k], B [256][k] as bf16 bit patterns (uint16)."""
+    lib = load()
+    a = np.ascontiguousarray(np.asarray(a_bits, dtype=np.uint16))
+    b = np.ascontiguousarray(np.asarray(b_bits, dtype=np.uint16))
+    m, k = a.shape
+    n = b.shape[0]
+    c = np.empty((m, n), dtype=np.float32)
+    st = lib.sp_gemm_bf16_nt(a.ctypes.data, b.ctypes.data, c.ctypes.data, m, n, k)
+    if st != 0:
+        raise SlideError(st, "sp_gemm_bf16_nt failed: %s" % lib.sp_status_string(st).decode())
+    return c
 
 
 def kernel_launch_count():
