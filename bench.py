@@ -181,9 +181,111 @@ def run_probe(args):
                       "idle_fraction": x["dev_idle_cycles"] / max(1, x["dev_warp_cycles"])}), flush=True)
 
 
+def _timed_solve(solver, states, reps=1):
+    """Best wall time of `reps` host-buffer solves (after one warm-up)."""
+    import torch
+    solver.solve_raw(states)
+    best, res, st = None, None, None
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = solver.solve_raw(states)
+        dt = time.perf_counter() - t0
+        if best is None or dt < best:
+            best, res, st = dt, r, solver.stats()
+    n = states.shape[0]
+    for i in range(n):
+        if res[i].status != 0:
+            raise RuntimeError("instance %d failed with status %d" % (i, res[i].status))
+    return best, [res[i] for i in range(n)], st
+
+
+def _summary(label, dt, res, st, extra=None):
+    nodes = sum(r.nodes_total for r in res)
+    lens = sorted(r.len for r in res)
+    lat = sorted(r.seconds for r in res)
+
+    def q(a, f):
+        return a[min(len(a) - 1, int(f * len(a)))]
+    d = {"workload": label, "instances": len(res), "seconds": dt, "nodes": nodes, "nodes_per_s": nodes / dt,
+         "instances_per_s": len(res) / dt, "kernel_ms": st["kernel_ms"], "rounds": st["rounds"],
+         "kernel_launches": st["kernel_launches"], "tasks_donated": st["tasks_donated"],
+         "lane_step_fraction": st["dev_lane_steps"] / max(1, st["dev_lane_slots"]),
+         "optimal_len": {"min": lens[0], "p50": q(lens, 0.5), "max": lens[-1]},
+         "latency_s": {"p50": q(lat, 0.5), "p99": q(lat, 0.99), "max": lat[-1]}}
+    if extra:
+        d.update(extra)
+    return d
+
+
+def run_workload(args):
+    """Secondary workloads (the other configurations of the benchmark plan),
+    one JSON line each; the headline line is the default mode."""
+    import torch
+    import instances
+    import slide
+    torch.cuda.set_device(0)
+    out = []
+    modes = [("round", 0), ("persistent", 1)]
+    if args.workload == "15_md_walk60":
+        w, states = instances.config_instances("15_md_walk60")
+        for name, pers in modes:
+            s = slide.Solver(w, "manhattan", lb_mode="static", persistent=pers)
+            dt, res, st = _timed_solve(s, states, reps=3)
+            out.append(_summary("15_md_walk60/" + name, dt, res, st, {"heuristic": "manhattan"}))
+            s.close()
+    elif args.workload == "15_mixed4096":
+        w, states = instances.config_instances("15_mixed4096")
+        for name, pers in modes:
+            s = slide.Solver(w, "pdb", lb_mode="static", persistent=pers, frontier_target=args.frontier)
+            s.build_pdb()
+            dt, res, st = _timed_solve(s, states, reps=2)
+            out.append(_summary("15_mixed4096/" + name, dt, res, st,
+                                {"heuristic": "pdb555", "frontier_target": args.frontier}))
+            s.close()
+    elif args.workload == "24_bins":
+        s = slide.Solver(5, "pdb", lb_mode="static", frontier_target=args.frontier)
+        t0 = time.perf_counter()
+        s.build_pdb()
+        pdb_s = time.perf_counter() - t0
+        for m in (120, 160, 200):
+            _, states = instances.config_instances("24_walk%d" % m)
+            dt, res, st = _timed_solve(s, states)
+            out.append(_summary("24_walk%d" % m, dt, res, st,
+                                {"heuristic": "pdb6666", "pdb_build_s": pdb_s, "frontier_target": args.frontier}))
+    elif args.workload == "lb_ab":
+        import train_lb
+        s = slide.Solver(5, "pdb", frontier_target=8192)
+        s.build_pdb()
+        t0 = time.perf_counter()
+        tiles, slack, target, mean = train_lb.make_dataset(s, args.tuples, 8, 0x1B, log=lambda m: None)
+        data_s = time.perf_counter() - t0
+        s.lbm_init(0x1B)
+        metrics = train_lb.train(s, tiles, slack, target, epochs=args.epochs, log=lambda m: None)
+        _, states = instances.config_instances("24_walk%d" % args.ab_bin)
+        rows = {}
+        for lb in ("static", "learned"):
+            s.set_config(lb_mode=lb, frontier_target=8192)
+            dt, res, st = _timed_solve(s, states)
+            rows[lb] = _summary("24_walk%d/%s" % (args.ab_bin, lb), dt, res, st)
+            rows[lb]["round_kernel_ms"] = [round(x, 2) for x in st["round_kernel_ms"]]
+        out.append({"workload": "lb_ab", "bin": "24_walk%d" % args.ab_bin, "frontier_target": 8192,
+                    "tuples": int(len(target)), "slack_mean_nodes": [float(x) for x in mean],
+                    "data_s": data_s, "model": metrics,
+                    "static_s": rows["static"]["seconds"], "learned_s": rows["learned"]["seconds"],
+                    "speedup_learned": rows["static"]["seconds"] / rows["learned"]["seconds"],
+                    "static": rows["static"], "learned": rows["learned"]})
+    for d in out:
+        print(json.dumps(d), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--probe", choices=["balanced"], default=None)
+    ap.add_argument("--workload", choices=["15_md_walk60", "15_mixed4096", "24_bins", "lb_ab"], default=None)
+    ap.add_argument("--tuples", type=int, default=1_000_000)
+    ap.add_argument("--epochs", type=int, default=3)
+    ap.add_argument("--ab-bin", type=int, default=200)
     ap.add_argument("--probe-heuristic", default="pdb", choices=["manhattan", "pdb"])
     ap.add_argument("--probe-width", type=int, default=4)
     ap.add_argument("--probe-slack", type=int, default=8)
@@ -195,12 +297,15 @@ def main():
     ap.add_argument("--instances", type=int, default=100)
     ap.add_argument("--frontier", type=int, default=2048)
     ap.add_argument("--lb", default="static")
+    ap.add_argument("--persistent", type=int, default=0, choices=[0, 1])
     ap.add_argument("--ref-seconds", type=float, default=8.0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.probe:
         return run_probe(args)
+    if args.workload:
+        return run_workload(args)
     if args.impl == "reference":
         return run_reference(args)
 
@@ -214,7 +319,7 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     w, states = workload(rank, args.instances)
     n = states.shape[0]
-    solver = slide.Solver(w, "pdb", frontier_target=args.frontier, lb_mode=args.lb)
+    solver = slide.Solver(w, "pdb", frontier_target=args.frontier, lb_mode=args.lb, persistent=args.persistent)
     t0 = time.perf_counter()
     solver.build_pdb()
     pdb_ms = 1000 * (time.perf_counter() - t0)
@@ -313,6 +418,7 @@ def main():
             "config": {"workload": "15puzzle_random100_pdb555", "instances_per_gpu": n,
                        "heuristic": "additive 5-5-5 PDB, max(regular, reflected)",
                        "frontier_target": args.frontier, "lb": args.lb + "+donation",
+                       "threshold_loop": "device (one launch)" if args.persistent else "host (one launch per round)",
                        "parallelism": "replicas" if world > 1 else "1 GPU",
                        "l2": "512 MB buffer written between timed steps",
                        "pdb_build_ms": round(pdb_ms, 2)},

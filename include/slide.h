@@ -95,7 +95,8 @@ typedef struct {
   int32_t f_limit[SP_MAX_ITERS];
   uint64_t nodes[SP_MAX_ITERS];
   uint8_t moves[SP_MAX_MOVES];
-  double seconds;            /* wall time of the batch this instance was in */
+  double seconds;            /* from the call's start until this instance's answer
+                                was final (the batch's wall time at most) */
 } sp_result;
 
 #define SP_MAX_ROUNDS 96

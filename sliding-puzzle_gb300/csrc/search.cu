@@ -148,6 +148,7 @@ __device__ __noinline__ void warp_advance(const RoundParams &P, uint32_t i, uint
     if (stop || r + 1 >= kMaxIters) {
       if (lane == 0) {
         P.inst_final[i] = r;
+        P.inst_fin_ns[i] = globaltimer();
         if (!stop) P.inst_status[i] = SP_ERR_LIMIT;
       }
       return;
@@ -268,6 +269,7 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
     s_pool[0] = s_pool[1] = s_pool[2] = s_pool[4] = 0;
     s_pool[3] = 1;
     s_pool_t = 0;
+    if (MULTI) atomicMin(P.t_begin_ns, globaltimer());
   }
 
   const HeurTables *ht = P.ht;

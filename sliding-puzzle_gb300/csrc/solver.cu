@@ -122,11 +122,13 @@ struct Pinned {
 struct MultiBufs {
   int32_t *iter = nullptr, *fin = nullptr, *status = nullptr, *goal = nullptr, *subf = nullptr, *ifv = nullptr;
   uint32_t *out = nullptr, *base = nullptr, *nsub = nullptr, *ioff = nullptr, *ilen = nullptr;
-  unsigned long long *icum = nullptr, *iter_nodes = nullptr, *loads = nullptr;
+  unsigned long long *icum = nullptr, *iter_nodes = nullptr, *loads = nullptr, *fin_ns = nullptr, *t0_ns = nullptr;
   size_t cap_iter = 0, cap_fin = 0, cap_status = 0, cap_goal = 0, cap_subf = 0, cap_ifv = 0, cap_out = 0,
-         cap_base = 0, cap_nsub = 0, cap_ioff = 0, cap_ilen = 0, cap_icum = 0, cap_iter_nodes = 0, cap_loads = 0;
+         cap_base = 0, cap_nsub = 0, cap_ioff = 0, cap_ilen = 0, cap_icum = 0, cap_iter_nodes = 0, cap_loads = 0,
+         cap_fin_ns = 0, cap_t0_ns = 0;
   void release() {
-    void *ptrs[] = {iter, fin, status, goal, subf, ifv, out, base, nsub, ioff, ilen, icum, iter_nodes, loads};
+    void *ptrs[] = {iter, fin,  status, goal, subf,       ifv,   out,    base,
+                    nsub, ioff, ilen,   icum, iter_nodes, loads, fin_ns, t0_ns};
     for (void *p : ptrs) cudaFree(p);
   }
 };
@@ -545,6 +547,8 @@ int launch_round(sp_solver *s, const RoundPlan &plan, size_t n_subs, size_t n_in
     P.goal_maxf = m.goal;
     P.iter_nodes = m.iter_nodes;
     P.sub_loads = m.loads;
+    P.inst_fin_ns = m.fin_ns;
+    P.t_begin_ns = m.t0_ns;
     P.n_subs = (uint32_t)n_subs;
     P.static_split = (s->cfg.lb_mode == SP_LB_STATIC_STEAL || s->cfg.lb_mode == SP_LB_LEARNED) ? 1 : 0;
     SP_CUDA(s, launch_search_multi(s->w, s->heur == SP_HEUR_PDB, block, s->cfg.blocks_per_sm, s->num_sms, P,
@@ -796,7 +800,8 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
       (rc = ensure(s, &m.goal, &m.cap_goal, ni)) || (rc = ensure(s, &m.subf, &m.cap_subf, h_subf.size())) ||
       (rc = ensure(s, &m.ifv, &m.cap_ifv, h_if.size())) || (rc = ensure(s, &m.icum, &m.cap_icum, h_icum.size())) ||
       (rc = ensure(s, &m.iter_nodes, &m.cap_iter_nodes, ni * kMaxIters)) ||
-      (rc = ensure(s, &m.loads, &m.cap_loads, 2 * std::max<size_t>(n_subs, 1))))
+      (rc = ensure(s, &m.loads, &m.cap_loads, 2 * std::max<size_t>(n_subs, 1))) ||
+      (rc = ensure(s, &m.fin_ns, &m.cap_fin_ns, ni)) || (rc = ensure(s, &m.t0_ns, &m.cap_t0_ns, 1)))
     return rc;
   auto up = [&](auto *dst, const auto &v) {
     return cudaMemcpyAsync(dst, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice, s->st);
@@ -817,7 +822,12 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
   SP_CUDA(s, cudaMemsetAsync(m.iter_nodes, 0, ni * kMaxIters * sizeof(unsigned long long), s->st));
   SP_CUDA(s, cudaMemsetAsync(m.loads, 0, 2 * std::max<size_t>(n_subs, 1) * sizeof(unsigned long long), s->st));
   SP_CUDA(s, cudaMemsetAsync(s->d_sol, 0, ni * sizeof(Solution), s->st));
+  SP_CUDA(s, cudaMemsetAsync(m.fin_ns, 0, ni * sizeof(unsigned long long), s->st));
+  SP_CUDA(s, cudaMemsetAsync(m.t0_ns, 0xFF, sizeof(unsigned long long), s->st));
   s->stats.h2d_bytes += ni * 40 + h_subf.size() * 4 + h_if.size() * 12;
+  const double pre_s = ms_since(t_start) / 1000.0;  // host part before the launch
+  for (auto &I : inst)
+    if (I.done) I.out->seconds = pre_s;
   float ms = 0;
   if (!direct.empty()) {
     RoundPlan plan;
@@ -845,7 +855,9 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
     }
   }
   std::vector<int32_t> fin(ni), st(ni);
-  std::vector<unsigned long long> itn(ni * kMaxIters);
+  std::vector<unsigned long long> itn(ni * kMaxIters), fin_ns(ni), t0(1, 0);
+  SP_CUDA(s, cudaMemcpyAsync(fin_ns.data(), m.fin_ns, ni * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s->st));
+  SP_CUDA(s, cudaMemcpyAsync(t0.data(), m.t0_ns, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s->st));
   SP_CUDA(s, cudaMemcpyAsync(fin.data(), m.fin, ni * sizeof(int32_t), cudaMemcpyDeviceToHost, s->st));
   SP_CUDA(s, cudaMemcpyAsync(st.data(), m.status, ni * sizeof(int32_t), cudaMemcpyDeviceToHost, s->st));
   SP_CUDA(s, cudaMemcpyAsync(itn.data(), m.iter_nodes, itn.size() * sizeof(unsigned long long),
@@ -871,6 +883,7 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
     }
     R->n_iter = r_end + 1;
     rounds = std::max(rounds, R->n_iter);
+    if (fin_ns[i] && fin_ns[i] >= t0[0]) R->seconds = pre_s + 1e-9 * (double)(fin_ns[i] - t0[0]);
     if (fin[i] < 0) {
       R->status = SP_ERR_TIMEOUT;
     } else if (st[i]) {
@@ -884,7 +897,8 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
   }
   s->stats.rounds = rounds;
   const double wall = ms_since(t_start);
-  for (auto &I : inst) I.out->seconds = wall / 1000.0;
+  for (auto &I : inst)
+    if (I.out->seconds == 0.0) I.out->seconds = wall / 1000.0;
   s->stats.wall_ms = wall;
   return SP_OK;
 }
@@ -1088,11 +1102,14 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
         I.done = true;
       }
     }
+    const double now_s = ms_since(t_start) / 1000.0;
+    for (auto &I : inst)
+      if (I.done && I.out->seconds == 0.0) I.out->seconds = now_s;
     s->stats.round_host_ms[ri] = (float)(ms_since(t_round) - s->stats.round_kernel_ms[ri]);
   }
   const double wall = ms_since(t_start);
   for (auto &I : inst) {
-    I.out->seconds = wall / 1000.0;
+    if (I.out->seconds == 0.0) I.out->seconds = wall / 1000.0;
     if (!I.done && I.out->status == SP_OK) I.out->status = SP_ERR_LIMIT;
   }
   s->stats.wall_ms = wall;

@@ -45,6 +45,8 @@ struct RoundParams {
   const int32_t *goal_maxf;           // smallest maxf of a root-set goal node (INT32_MAX: none)
   unsigned long long *iter_nodes;     // [instance][kMaxIters] generated nodes
   unsigned long long *sub_loads;      // [2][n_subs] per-root loads of the last two iterations
+  unsigned long long *inst_fin_ns;    // %globaltimer when the instance's answer became final
+  unsigned long long *t_begin_ns;     // %globaltimer at the launch's first block start (atomicMin)
   uint32_t n_subs;
   int32_t static_split;
 };
