@@ -210,6 +210,7 @@ def _summary(label, dt, res, st, extra=None):
     d = {"workload": label, "instances": len(res), "seconds": dt, "nodes": nodes, "nodes_per_s": nodes / dt,
          "instances_per_s": len(res) / dt, "kernel_ms": st["kernel_ms"], "rounds": st["rounds"],
          "kernel_launches": st["kernel_launches"], "tasks_donated": st["tasks_donated"],
+         "frontier_ms": st["frontier_ms"],
          "lane_step_fraction": st["dev_lane_steps"] / max(1, st["dev_lane_slots"]),
          "optimal_len": {"min": lens[0], "p50": q(lens, 0.5), "max": lens[-1]},
          "latency_s": {"p50": q(lat, 0.5), "p99": q(lat, 0.99), "max": lat[-1]}}
@@ -255,18 +256,24 @@ def run_workload(args):
                                 {"heuristic": "pdb6666", "pdb_build_s": pdb_s, "frontier_target": args.frontier}))
     elif args.workload == "lb_ab":
         import train_lb
+
+        def log(m):
+            print("[lb_ab %.1fs] %s" % (time.perf_counter() - t_start, m), file=sys.stderr, flush=True)
+        t_start = time.perf_counter()
         s = slide.Solver(5, "pdb", frontier_target=8192)
         s.build_pdb()
         t0 = time.perf_counter()
-        tiles, slack, target, mean = train_lb.make_dataset(s, args.tuples, 8, 0x1B, log=lambda m: None)
+        tiles, slack, target, mean = train_lb.make_dataset(s, args.tuples, 8, 0x1B, log=log)
         data_s = time.perf_counter() - t0
         s.lbm_init(0x1B)
-        metrics = train_lb.train(s, tiles, slack, target, epochs=args.epochs, log=lambda m: None)
+        metrics = train_lb.train(s, tiles, slack, target, epochs=args.epochs, log=log)
+        log("model %s" % metrics)
         _, states = instances.config_instances("24_walk%d" % args.ab_bin)
         rows = {}
         for lb in ("static", "learned"):
             s.set_config(lb_mode=lb, frontier_target=8192)
             dt, res, st = _timed_solve(s, states)
+            log("%s solve %.2f s" % (lb, dt))
             rows[lb] = _summary("24_walk%d/%s" % (args.ab_bin, lb), dt, res, st)
             rows[lb]["round_kernel_ms"] = [round(x, 2) for x in st["round_kernel_ms"]]
         out.append({"workload": "lb_ab", "bin": "24_walk%d" % args.ab_bin, "frontier_target": 8192,

@@ -69,7 +69,12 @@ def make_dataset(solver, n, smax, seed, node_budget=2e11, chunk=1 << 16, log=pri
     width = solver.width
     lo, hi = (100, 220) if width == 5 else (40, 80)
     probe = vector_walks(width, 2048, lo, hi, seed ^ 0x5EED)
-    mean = np.array([max(1.0, float(label(solver, probe, np.full(2048, s)).mean())) for s in range(smax + 1)])
+    mean = []
+    for s in range(smax + 1):
+        t0 = time.time()
+        mean.append(max(1.0, float(label(solver, probe, np.full(2048, s)).mean())))
+        log("probe slack %d: %.3g nodes/root (%.2f s)" % (s, mean[-1], time.time() - t0))
+    mean = np.array(mean)
     w = 1.0 / mean
     share = np.minimum(w / w.sum() * n, np.full(smax + 1, n / (smax + 1.0) * 2))
     share = np.maximum(share, 1)
@@ -87,13 +92,18 @@ def make_dataset(solver, n, smax, seed, node_budget=2e11, chunk=1 << 16, log=pri
     tiles = np.empty((total, width * width), dtype=np.uint8)
     target = np.empty(total, dtype=np.float32)
     t0 = time.time()
+    t_walk = t_label = 0.0
     for off in range(0, total, chunk):
         m = min(chunk, total - off)
+        ta = time.time()
         st = vector_walks(width, m, lo, hi, seed + 1 + off)
+        tb = time.time()
         nodes = label(solver, st, slack[off:off + m])
+        t_walk += tb - ta
+        t_label += time.time() - tb
         tiles[off:off + m] = st
         target[off:off + m] = np.log2(1.0 + nodes.astype(np.float64))
-    log("labelled %d tuples in %.1f s" % (total, time.time() - t0))
+    log("labelled %d tuples in %.1f s (walks %.1f s, search %.1f s)" % (total, time.time() - t0, t_walk, t_label))
     return tiles, slack.astype(np.int32), target, mean
 
 
