@@ -263,7 +263,7 @@ def run_workload(args):
         s = slide.Solver(5, "pdb", frontier_target=8192)
         s.build_pdb()
         t0 = time.perf_counter()
-        tiles, slack, target, mean = train_lb.make_dataset(s, args.tuples, 8, 0x1B, log=log)
+        tiles, slack, target, mean = train_lb.make_dataset(s, args.tuples, 7, 0x1B, log=log)
         data_s = time.perf_counter() - t0
         s.lbm_init(0x1B)
         metrics = train_lb.train(s, tiles, slack, target, epochs=args.epochs, log=log)

@@ -64,26 +64,23 @@ def label(solver, states, slack):
 
 
 def make_dataset(solver, n, smax, seed, node_budget=2e11, chunk=1 << 16, log=print):
-    """About n tuples; slack values share the node budget evenly (large slacks
-    are rarer), and the tuple count shrinks if the budget would be exceeded."""
+    """Up to n tuples spread evenly over slack 0..smax, except that no slack
+    value may cost more than its share of the node budget (subtrees grow
+    about 9x per slack step on the 24-puzzle, so large slacks get fewer)."""
     width = solver.width
     lo, hi = (100, 220) if width == 5 else (40, 80)
     probe = vector_walks(width, 2048, lo, hi, seed ^ 0x5EED)
-    mean = []
+    mean, prev = [], 1.0
     for s in range(smax + 1):
+        # probe size: about 2e10 nodes at most, from the previous slack's mean
+        m = int(min(2048, max(32, 2e10 / (prev * 10.0))))
         t0 = time.time()
-        mean.append(max(1.0, float(label(solver, probe, np.full(2048, s)).mean())))
-        log("probe slack %d: %.3g nodes/root (%.2f s)" % (s, mean[-1], time.time() - t0))
+        prev = max(1.0, float(label(solver, probe[:m], np.full(m, s)).mean()))
+        mean.append(prev)
+        log("probe slack %d: %.3g nodes/root over %d roots (%.2f s)" % (s, prev, m, time.time() - t0))
     mean = np.array(mean)
-    w = 1.0 / mean
-    share = np.minimum(w / w.sum() * n, np.full(smax + 1, n / (smax + 1.0) * 2))
-    share = np.maximum(share, 1)
-    counts = np.floor(share / share.sum() * n).astype(np.int64)
-    counts[0] += n - counts.sum()
-    est = float((counts * mean).sum())
-    if est > node_budget:
-        counts = np.maximum(1, (counts * (node_budget / est)).astype(np.int64))
-    log("slack mean nodes: %s" % ", ".join("%d:%.3g" % (s, m) for s, m in enumerate(mean)))
+    per = n / (smax + 1.0)
+    counts = np.maximum(1, np.minimum(per, node_budget / (smax + 1.0) / mean)).astype(np.int64)
     log("tuples per slack: %s (about %.3g nodes)" % (counts.tolist(), float((counts * mean).sum())))
     slack = np.repeat(np.arange(smax + 1), counts)
     rng = np.random.default_rng(seed)
@@ -144,7 +141,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--width", type=int, default=5)
     ap.add_argument("--tuples", type=int, default=2_000_000)
-    ap.add_argument("--smax", type=int, default=8)
+    ap.add_argument("--smax", type=int, default=7)
     ap.add_argument("--epochs", type=int, default=3)
     ap.add_argument("--seed", type=int, default=0x1B)
     ap.add_argument("--budget", type=float, default=2e11)
