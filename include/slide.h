@@ -70,7 +70,9 @@ typedef enum {
 } sp_lb_mode;
 
 typedef struct {
-  int32_t frontier_target;   /* subproblems per instance (reference BLOCK_NUM 2048) */
+  int32_t frontier_target;   /* subproblems per instance (reference BLOCK_NUM 2048);
+                                a batch is capped near 8 per resident GPU lane
+                                (at least 32 per instance) */
   int32_t threads_per_block; /* 128 or 256 */
   int32_t blocks_per_sm;     /* 0 = occupancy maximum */
   int32_t lb_mode;           /* sp_lb_mode */

@@ -934,7 +934,13 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
   // root set: uniform-depth tree expansion to >= frontier_target leaves,
   // instances spread over host threads
   auto t_front = std::chrono::steady_clock::now();
-  const int target = std::max(1, s->cfg.frontier_target);
+  // a batch's root set is capped near 8 roots per resident lane: more roots
+  // than that add host work and no balance (donation splits what is left)
+  size_t live = 0;
+  for (auto &I : inst) live += !I.done;
+  const double lanes = s->last_lanes > 0 ? (double)s->last_lanes : (double)s->num_sms * 768.0;
+  int target = std::max(1, s->cfg.frontier_target);
+  if (live) target = std::min(target, std::max(32, (int)(8.0 * lanes / (double)live)));
   auto build_tree = [&](Instance &I) {
     if (I.done) return;
     I.tree.reserve((size_t)target * 4 + 16);
