@@ -23,13 +23,17 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstdio>
+#include <functional>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -67,6 +71,7 @@ struct Instance {
   // round are a prefix), interior nodes as (maxf, cumulative children)
   std::vector<int32_t> leaves;
   std::vector<int32_t> leaf_maxf;
+  std::vector<uint8_t> leaf_g;       // depth of each leaf, same order
   std::vector<std::pair<int32_t, uint64_t>> interior;
   std::vector<int32_t> goals;        // tree nodes with h == 0
   std::vector<uint64_t> last_load;   // per leaf, previous round
@@ -286,22 +291,76 @@ void expand_node(int w, std::vector<TreeNode> &tree, int idx) {
   tree[(size_t)idx].leaf = 0;
 }
 
-// fn(i) for i in [0, n) on up to 16 host threads (instances are independent)
+// Host worker threads, created once and kept for the process (never joined:
+// a library must not block at exit on its own threads).  run(n, fn) calls
+// fn(i) for i in [0, n) on the workers and the caller; one run at a time.
+class WorkPool {
+ public:
+  static WorkPool &get() {
+    static WorkPool *pool = new WorkPool(std::max(1u, std::min(16u, std::thread::hardware_concurrency())) - 1);
+    return *pool;
+  }
+  // 0 in a forked child: it inherits this object but none of the threads
+  unsigned workers() const { return getpid() == pid_ ? (unsigned)threads_.size() : 0u; }
+  void run(size_t n, const std::function<void(size_t)> &fn) {
+    std::lock_guard<std::mutex> one(run_m_);
+    {
+      std::lock_guard<std::mutex> l(m_);
+      job_ = &fn;
+      n_ = n;
+      next_.store(0);
+      active_ = (int)threads_.size();
+      ++gen_;
+    }
+    cv_.notify_all();
+    for (size_t i; (i = next_.fetch_add(1)) < n;) fn(i);
+    std::unique_lock<std::mutex> l(m_);
+    done_cv_.wait(l, [&] { return active_ == 0; });
+  }
+
+ private:
+  explicit WorkPool(unsigned k) : pid_(getpid()) {
+    for (unsigned t = 0; t < k; ++t) threads_.emplace_back([this] { loop(); });
+    for (auto &t : threads_) t.detach();
+  }
+  void loop() {
+    uint64_t seen = 0;
+    for (;;) {
+      const std::function<void(size_t)> *job;
+      size_t n;
+      {
+        std::unique_lock<std::mutex> l(m_);
+        cv_.wait(l, [&] { return gen_ != seen; });
+        seen = gen_;
+        job = job_;
+        n = n_;
+      }
+      for (size_t i; (i = next_.fetch_add(1)) < n;) (*job)(i);
+      std::lock_guard<std::mutex> l(m_);
+      if (--active_ == 0) done_cv_.notify_one();
+    }
+  }
+  pid_t pid_;
+  std::vector<std::thread> threads_;
+  std::mutex run_m_, m_;
+  std::condition_variable cv_, done_cv_;
+  uint64_t gen_ = 0;
+  size_t n_ = 0;
+  std::atomic<size_t> next_{0};
+  int active_ = 0;
+  const std::function<void(size_t)> *job_ = nullptr;
+};
+
+// fn(i) for i in [0, n) on the host worker pool (instances are independent);
+// small n runs inline
 template <typename F>
 void parallel_for(size_t n, F fn) {
-  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-  const unsigned nt = (unsigned)std::min<size_t>(hw, std::max<size_t>(1, n / 4));
-  if (nt <= 1) {
+  if (n < 8 || WorkPool::get().workers() == 0) {
     for (size_t i = 0; i < n; ++i) fn(i);
     return;
   }
-  std::atomic<size_t> next{0};
-  std::vector<std::thread> pool;
-  for (unsigned t = 0; t < nt; ++t)
-    pool.emplace_back([&]() {
-      for (size_t i; (i = next.fetch_add(1)) < n;) fn(i);
-    });
-  for (auto &th : pool) th.join();
+  const std::function<void(size_t)> f = fn;
+  WorkPool::get().run(n, f);
 }
 
 uint8_t count_children(int w, const TreeNode &t) {
@@ -324,9 +383,12 @@ int finish_trees(sp_solver *s, std::vector<Instance> &inst) {
   Pinned<int32_t> &hv = s->h_hv;
   SP_CUDA(s, boards.reserve(total * (size_t)s->n));
   SP_CUDA(s, hv.reserve(total));
-  size_t o = 0;
-  for (auto &I : inst)
-    for (auto &t : I.tree) memcpy(boards.p + (o++) * s->n, t.board, (size_t)s->n);
+  std::vector<size_t> first(inst.size() + 1, 0);
+  for (size_t i = 0; i < inst.size(); ++i) first[i + 1] = first[i] + inst[i].tree.size();
+  parallel_for(inst.size(), [&](size_t i) {
+    size_t o = first[i];
+    for (auto &t : inst[i].tree) memcpy(boards.p + (o++) * s->n, t.board, (size_t)s->n);
+  });
   SP_CUDA(s, cudaMemcpyAsync(s->d_boards, boards.p, total * s->n, cudaMemcpyHostToDevice, s->st));
   s->stats.h2d_bytes += total * s->n;
   SP_CUDA(s, launch_heuristic(s->w, s->heur == SP_HEUR_PDB, s->d_boards, (int)total, s->d_h, s->d_ht,
@@ -334,8 +396,6 @@ int finish_trees(sp_solver *s, std::vector<Instance> &inst) {
   SP_CUDA(s, cudaMemcpyAsync(hv.p, s->d_h, total * sizeof(int32_t), cudaMemcpyDeviceToHost, s->st));
   SP_CUDA(s, cudaStreamSynchronize(s->st));
   s->stats.d2h_bytes += total * sizeof(int32_t);
-  std::vector<size_t> first(inst.size() + 1, 0);
-  for (size_t i = 0; i < inst.size(); ++i) first[i + 1] = first[i] + inst[i].tree.size();
   parallel_for(inst.size(), [&](size_t i) {
     Instance &I = inst[i];
     size_t o = first[i];
@@ -358,7 +418,11 @@ int finish_trees(sp_solver *s, std::vector<Instance> &inst) {
     std::stable_sort(I.leaves.begin(), I.leaves.end(),
                      [&](int32_t a, int32_t b) { return I.tree[(size_t)a].maxf < I.tree[(size_t)b].maxf; });
     I.leaf_maxf.resize(I.leaves.size());
-    for (size_t q = 0; q < I.leaves.size(); ++q) I.leaf_maxf[q] = I.tree[(size_t)I.leaves[q]].maxf;
+    I.leaf_g.resize(I.leaves.size());
+    for (size_t q = 0; q < I.leaves.size(); ++q) {
+      I.leaf_maxf[q] = I.tree[(size_t)I.leaves[q]].maxf;
+      I.leaf_g[q] = I.tree[(size_t)I.leaves[q]].g;
+    }
     std::sort(interior.begin(), interior.end());
     I.interior.clear();
     uint64_t cum = 0;
@@ -590,77 +654,103 @@ int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int3
                RoundPlan &plan) {
   const bool learned = s->cfg.lb_mode == SP_LB_LEARNED;
   const bool stat = s->cfg.lb_mode == SP_LB_STATIC_STEAL || learned;
-  struct Cand {
-    double pred;
-    uint32_t sub;
-    int room;  // levels left below the root before the limit
-  };
-  std::vector<Cand> c;
-  std::vector<uint32_t> q_sub, q_pos;  // roots for the model
-  std::vector<int32_t> q_slack;
-  double total = 0;
-  for (size_t i = 0; i < inst.size(); ++i) {
+  // candidates: the active roots of every live instance, instance by instance
+  const size_t ni = inst.size();
+  std::vector<size_t> off(ni + 1, 0);
+  for (size_t i = 0; i < ni; ++i)
+    off[i + 1] = off[i] + (inst[i].done ? 0 : active_leaves(inst[i], limits[i]));
+  const size_t nc = off[ni];
+  if (!stat) {
+    plan.direct.resize(nc);
+    parallel_for(ni, [&](size_t i) {
+      for (size_t q = 0; q < off[i + 1] - off[i]; ++q) plan.direct[off[i] + q] = inst[i].sub_base + (uint32_t)q;
+    });
+    return SP_OK;
+  }
+  std::vector<double> pred(nc), inst_total(ni, 0.0);
+  std::vector<uint32_t> csub(nc);
+  std::vector<int16_t> room(nc);  // levels left below the root before the limit
+  parallel_for(ni, [&](size_t i) {
     Instance &I = inst[i];
-    if (I.done) continue;
-    const size_t na = active_leaves(I, limits[i]);
-    if (!stat) {
-      for (size_t q = 0; q < na; ++q) plan.direct.push_back(I.sub_base + (uint32_t)q);
-      continue;
-    }
+    const size_t na = off[i + 1] - off[i];
+    if (!na) return;
     double growth = 6.0;
     if (I.prev_total > 0 && I.last_total > 0)
       growth = std::min(30.0, std::max(2.0, (double)I.last_total / (double)I.prev_total));
+    double tot = 0;
     for (size_t q = 0; q < na; ++q) {
-      const TreeNode &t = I.tree[(size_t)I.leaves[q]];
       const double p = (double)I.last_load[q] * growth;
-      if (learned && I.last_load[q] == 0) {
+      pred[off[i] + q] = p;
+      csub[off[i] + q] = I.sub_base + (uint32_t)q;
+      room[off[i] + q] = (int16_t)(limits[i] - (int)I.leaf_g[q]);
+      tot += p;
+    }
+    inst_total[i] = tot;
+  });
+  double total = 0;
+  for (double t : inst_total) total += t;
+  if (learned) {
+    // roots without a measured load: the model's prediction at this threshold
+    std::vector<uint32_t> q_sub, q_pos;
+    std::vector<int32_t> q_slack;
+    for (size_t i = 0; i < ni; ++i) {
+      const Instance &I = inst[i];
+      for (size_t q = 0; q < off[i + 1] - off[i]; ++q) {
+        if (I.last_load[q]) continue;
+        const TreeNode &t = I.tree[(size_t)I.leaves[q]];
         q_sub.push_back(I.sub_base + (uint32_t)q);
-        q_pos.push_back((uint32_t)c.size());
+        q_pos.push_back((uint32_t)(off[i] + q));
         q_slack.push_back(std::max(0, (limits[i] - (int)t.g - t.h) / 2));
       }
-      c.push_back({p, I.sub_base + (uint32_t)q, limits[i] - (int)t.g});
-      total += p;
     }
-  }
-  if (!stat) return SP_OK;
-  if (!q_sub.empty()) {
-    std::vector<float> y(q_sub.size());
-    int rc = s->lbm->predict_subs(s->d_subs, q_sub.data(), q_slack.data(), (int)q_sub.size(), y.data(), s->st,
-                                  s->err);
-    if (rc) return rc;
-    s->stats.kernel_launches += 2 * (int)((q_sub.size() + 65535) / 65536);
-    for (size_t k = 0; k < q_sub.size(); ++k) {
-      const double p = std::exp2(std::min(60.0, std::max(0.0, (double)y[k]))) - 1.0;
-      c[q_pos[k]].pred = p;
-      total += p;
+    if (!q_sub.empty()) {
+      std::vector<float> y(q_sub.size());
+      int rc = s->lbm->predict_subs(s->d_subs, q_sub.data(), q_slack.data(), (int)q_sub.size(), y.data(), s->st,
+                                    s->err);
+      if (rc) return rc;
+      s->stats.kernel_launches += 2 * (int)((q_sub.size() + 65535) / 65536);
+      for (size_t k = 0; k < q_sub.size(); ++k) {
+        const double p = std::exp2(std::min(60.0, std::max(0.0, (double)y[k]))) - 1.0;
+        pred[q_pos[k]] = p;
+        total += p;
+      }
     }
   }
   const double lanes = s->last_lanes > 0 ? (double)s->last_lanes : (double)s->num_sms * 1024.0;
   const double T = total / (lanes * 4.0);
   static const size_t pow3[12] = {1, 3, 9, 27, 81, 243, 729, 2187, 6561, 19683, 59049, 177147};
   auto bound = [&](int kk) { return kk ? 4 * pow3[kk - 1] : (size_t)0; };
-  std::vector<int> k(c.size(), 0);
   const int kcap = std::min(10, std::max(1, s->cfg.static_split_cap));
+  // exponent of pred relative to T (ceil(log2(pred/T)) for pred > T): the
+  // split depth and the bucket of the longest-first order (bucket 63 - e:
+  // larger predictions first)
+  std::vector<int8_t> k(nc, 0);
+  std::vector<uint8_t> bucket(nc, 127);
+  const size_t nchunk = std::max<size_t>(1, std::min<size_t>(64, nc / 8192));
+  auto chunk_lo = [&](size_t c) { return nc * c / nchunk; };
+  std::vector<size_t> need_c(nchunk, 0);
+  parallel_for(nchunk, [&](size_t c) {
+    size_t need = 0;
+    for (size_t j = chunk_lo(c); j < chunk_lo(c + 1); ++j) {
+      int e = -64;
+      if (pred[j] > 0 && T > 0) {
+        std::frexp(pred[j] / T, &e);  // pred/T in [2^(e-1), 2^e)
+        e = std::max(-63, std::min(63, e));
+      }
+      bucket[j] = (uint8_t)(63 - e);
+      if (T > 0 && pred[j] > T) {
+        k[j] = (int8_t)std::max(0, std::min(e, std::min(kcap, (int)room[j] - 1)));
+        need += bound(k[j]);
+      }
+    }
+    need_c[c] = need;
+  });
   size_t need = 0;
-  // exponent of pred relative to T (ceil(log2(pred/T)) for pred > T), also the
-  // bucket of the longest-first order
-  std::vector<int8_t> ex(c.size(), 0);
-  for (size_t j = 0; j < c.size(); ++j) {
-    int e = -64;
-    if (c[j].pred > 0 && T > 0) {
-      std::frexp(c[j].pred / T, &e);  // pred/T in [2^(e-1), 2^e)
-      e = std::max(-63, std::min(63, e));
-    }
-    ex[j] = (int8_t)e;
-    if (T > 0 && c[j].pred > T) {
-      k[j] = std::max(0, std::min(e, std::min(kcap, c[j].room - 1)));
-      need += bound(k[j]);
-    }
-  }
+  for (size_t x : need_c) need += x;
   const size_t budget = (size_t)1 << 22;
   while (need > budget) {  // trim the deepest splits first
     int mk = 0;
-    for (int kk : k) mk = std::max(mk, kk);
+    for (int8_t kk : k) mk = std::max(mk, (int)kk);
     if (!mk) break;
     for (auto &kk : k)
       if (kk == mk) {
@@ -668,28 +758,42 @@ int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int3
         --kk;
       }
   }
-  // longest first: counting sort on the exponent (descending), stable within
-  std::vector<uint32_t> order(c.size());
-  {
-    size_t cnt[129] = {0};
-    for (int8_t e : ex) ++cnt[63 - e + 1];
-    for (int b = 1; b < 129; ++b) cnt[b] += cnt[b - 1];
-    for (size_t j = 0; j < c.size(); ++j) order[cnt[63 - ex[j]]++] = (uint32_t)j;
-  }
-  size_t level[12] = {0};
-  for (uint32_t j : order) {
-    if (k[j] > 0) {
-      Task t{};
-      t.sub = c[j].sub;
-      t.mask = 0xF;
-      t.flags = (uint8_t)k[j];
-      plan.split.push_back(t);
-      plan.max_k = std::max(plan.max_k, k[j]);
-      for (int l = 1; l <= k[j]; ++l) level[l] += 4 * pow3[l - 1];
-      plan.emit_bound += bound(k[j]);
-    } else {
-      plan.direct.push_back(c[j].sub);
+  // stable counting sort by bucket, split roots and whole roots separately:
+  // per-chunk histograms, then every chunk scatters into its own ranges
+  std::vector<uint32_t> hd(nchunk * 128, 0), hs(nchunk * 128, 0);
+  parallel_for(nchunk, [&](size_t c) {
+    for (size_t j = chunk_lo(c); j < chunk_lo(c + 1); ++j) ++(k[j] > 0 ? hs : hd)[c * 128 + bucket[j]];
+  });
+  size_t nd = 0, nsp = 0;
+  for (int b = 0; b < 128; ++b)
+    for (size_t c = 0; c < nchunk; ++c) {
+      const uint32_t a = hd[c * 128 + b], z = hs[c * 128 + b];
+      hd[c * 128 + b] = (uint32_t)nd;
+      hs[c * 128 + b] = (uint32_t)nsp;
+      nd += a;
+      nsp += z;
     }
+  plan.direct.resize(nd);
+  plan.split.resize(nsp);
+  parallel_for(nchunk, [&](size_t c) {
+    for (size_t j = chunk_lo(c); j < chunk_lo(c + 1); ++j) {
+      if (k[j] > 0) {
+        Task t{};
+        t.sub = csub[j];
+        t.mask = 0xF;
+        t.flags = (uint8_t)k[j];
+        plan.split[hs[c * 128 + bucket[j]]++] = t;
+      } else {
+        plan.direct[hd[c * 128 + bucket[j]]++] = csub[j];
+      }
+    }
+  });
+  size_t level[12] = {0};
+  for (const Task &t : plan.split) {
+    const int kk = t.flags;
+    plan.max_k = std::max(plan.max_k, kk);
+    for (int l = 1; l <= kk; ++l) level[l] += 4 * pow3[l - 1];
+    plan.emit_bound += bound(kk);
   }
   for (int l = 1; l < 12; ++l) plan.level_bound = std::max(plan.level_bound, level[l]);
   return SP_OK;
@@ -961,23 +1065,12 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
   int rc = finish_trees(s, inst);
   if (rc) return rc;
   // SubRoot array: the leaves of every instance, in maxf order
-  std::vector<SubRoot> subs;
+  size_t n_subs = 0;
   for (size_t i = 0; i < inst.size(); ++i) {
     Instance &I = inst[i];
-    I.sub_base = (uint32_t)subs.size();
-    if (I.done) continue;
-    for (int32_t x : I.leaves) {
-      const TreeNode &t = I.tree[(size_t)x];
-      SubRoot r{};
-      memcpy(r.board, t.board, (size_t)n);
-      r.blank = t.blank;
-      r.g = t.g;
-      r.pre = t.pre;
-      r.inst = (uint32_t)i;
-      subs.push_back(r);
-    }
+    I.sub_base = (uint32_t)n_subs;
+    if (!I.done) n_subs += I.leaves.size();
   }
-  const size_t n_subs = subs.size();
   rc = ensure(s, &s->d_subs, &s->subs_cap, std::max<size_t>(n_subs, 1));
   if (rc) return rc;
   rc = ensure(s, &s->d_sub_nodes, &s->sub_nodes_cap, std::max<size_t>(n_subs, 1));
@@ -985,7 +1078,21 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
   if (n_subs) {
     Pinned<SubRoot> &hs = s->h_subs;
     SP_CUDA(s, hs.reserve(n_subs));
-    memcpy(hs.p, subs.data(), n_subs * sizeof(SubRoot));
+    parallel_for(inst.size(), [&](size_t i) {
+      const Instance &I = inst[i];
+      if (I.done) return;
+      SubRoot *out = hs.p + I.sub_base;
+      for (int32_t x : I.leaves) {
+        const TreeNode &t = I.tree[(size_t)x];
+        SubRoot r{};
+        memcpy(r.board, t.board, (size_t)n);
+        r.blank = t.blank;
+        r.g = t.g;
+        r.pre = t.pre;
+        r.inst = (uint32_t)i;
+        *out++ = r;
+      }
+    });
     SP_CUDA(s, cudaMemcpyAsync(s->d_subs, hs.p, n_subs * sizeof(SubRoot), cudaMemcpyHostToDevice, s->st));
     SP_CUDA(s, cudaStreamSynchronize(s->st));
     s->stats.h2d_bytes += n_subs * sizeof(SubRoot);
@@ -1049,18 +1156,25 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
       sols = s->h_sols.p;
     }
     ++s->stats.rounds;
-    // fold results
-    for (size_t i = 0; i < inst.size(); ++i) {
+    // fold results: per-root loads (parallel over instances), then the rest
+    std::vector<uint64_t> dev_nodes(inst.size(), 0);
+    parallel_for(inst.size(), [&](size_t i) {
       Instance &I = inst[i];
-      if (I.done) continue;
-      const int L = limits[i];
-      const size_t na = active_leaves(I, L);
+      if (I.done) return;
+      const size_t na = active_leaves(I, limits[i]);
       uint64_t dev = 0;
       for (size_t q = 0; q < na; ++q) {
         const uint64_t v = sn ? sn[I.sub_base + q] : 0;
         dev += v;
         I.last_load[q] = v;
       }
+      dev_nodes[i] = dev;
+    });
+    for (size_t i = 0; i < inst.size(); ++i) {
+      Instance &I = inst[i];
+      if (I.done) continue;
+      const int L = limits[i];
+      const uint64_t dev = dev_nodes[i];
       const uint64_t nodes = interior_nodes(I, L) + dev;
       I.prev_total = I.last_total;
       I.last_total = dev;
