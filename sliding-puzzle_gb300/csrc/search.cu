@@ -258,6 +258,11 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
   __shared__ int8_t s_mdd[PDB ? 1 : 4 * N * N];
   __shared__ uint32_t s_stack[WORDS][BLOCK];
   __shared__ uint32_t s_prefix[kPathWords][BLOCK];  // the lane's task prefix (its pool slot is freed)
+  // PDB: the two pattern values (regular, reflected) a descent overwrote, per
+  // level, so that backtracking restores them without table lookups; levels
+  // from HSAVE on look them up again
+  constexpr int HSAVE = PDB ? (W == 4 ? 64 : 32) : 1;
+  __shared__ uint16_t s_hsave[HSAVE][BLOCK];
   __shared__ __align__(16) uint8_t s_board[W == 5 ? BLOCK * BSTRIDE : 4];
   // multi-iteration mode: per-warp bucket counts of the longest-first publication
   __shared__ uint32_t s_hist[MULTI ? BLOCK / 32 : 1][32];
@@ -523,7 +528,16 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
         blank = src;
         ++g;
         h = nh;
-        if (PDB) { ir = nir; iff = nif; hvr = nhvr; hvf = nhvf; }
+        if (PDB) {
+          if (k < HSAVE) {
+            const int pr = s_pat[t], pf = s_pat[N + t];
+            s_hsave[k][tid] = (uint16_t)(((hvr >> (8 * pr)) & 0xFFu) | (((hvf >> (8 * pf)) & 0xFFu) << 8));
+          }
+          ir = nir;
+          iff = nif;
+          hvr = nhvr;
+          hvf = nhvf;
+        }
         const int sh = 2 * (k & 15);
         top = (top & ~(3u << sh)) | ((uint32_t)d << sh);
         if ((k & 15) == 15) s_stack[k >> 4][tid] = top;
@@ -555,8 +569,14 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
       const int pr = s_pat[t], pf = s_pat[N + t];
       ir.add(pr, (int32_t)(s_code[t * N + blank] - s_code[t * N + back]));
       iff.add(pf, (int32_t)(s_code[N * N + t * N + blank] - s_code[N * N + t * N + back]));
-      hvr = set_byte(hvr, pr, lookup(W == 5 ? (pr != 0) : pr, ir.get(pr)));
-      hvf = set_byte(hvf, pf, lookup(W == 5 ? (pf != 0) : pf, iff.get(pf)));
+      if (k < HSAVE) {
+        const uint32_t sv = s_hsave[k][tid];
+        hvr = set_byte(hvr, pr, sv & 0xFFu);
+        hvf = set_byte(hvf, pf, sv >> 8);
+      } else {
+        hvr = set_byte(hvr, pr, lookup(W == 5 ? (pr != 0) : pr, ir.get(pr)));
+        hvf = set_byte(hvf, pf, lookup(W == 5 ? (pf != 0) : pf, iff.get(pf)));
+      }
       h = (int)max(byte_sum(hvr), byte_sum(hvf));
     } else {
       h -= s_mdd[(d * N + blank) * N + t];
