@@ -305,6 +305,9 @@ def main():
     ap.add_argument("--frontier", type=int, default=2048)
     ap.add_argument("--lb", default="static")
     ap.add_argument("--persistent", type=int, default=0, choices=[0, 1])
+    ap.add_argument("--autotune", action="store_true",
+                    help="pick block size, poll interval, persistence and donation reserve first "
+                         "(the root-set size stays the configured one)")
     ap.add_argument("--ref-seconds", type=float, default=8.0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -330,6 +333,10 @@ def main():
     t0 = time.perf_counter()
     solver.build_pdb()
     pdb_ms = 1000 * (time.perf_counter() - t0)
+    tuned = None
+    if args.autotune:
+        space = tuple(p for p in slide.AUTOTUNE_SPACE if p[0] != "frontier_target")
+        tuned, _ = slide.autotune(solver, states, space=space, reps=2)
     d_tiles = torch.from_numpy(states.copy()).to("cuda")
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
 
@@ -425,7 +432,10 @@ def main():
             "config": {"workload": "15puzzle_random100_pdb555", "instances_per_gpu": n,
                        "heuristic": "additive 5-5-5 PDB, max(regular, reflected)",
                        "frontier_target": args.frontier, "lb": args.lb + "+donation",
-                       "threshold_loop": "device (one launch)" if args.persistent else "host (one launch per round)",
+                       "threshold_loop": ("device (one launch)" if (tuned or {}).get("persistent", args.persistent)
+                                          else "host (one launch per round)"),
+                       "autotuned": {k: tuned[k] for k in ("threads_per_block", "steps_per_poll", "persistent",
+                                                           "donate_reserve")} if tuned else None,
                        "parallelism": "replicas" if world > 1 else "1 GPU",
                        "l2": "512 MB buffer written between timed steps",
                        "pdb_build_ms": round(pdb_ms, 2)},

@@ -303,6 +303,71 @@ def result_dict(r):
     }
 
 
+AUTOTUNE_SPACE = (
+    ("threads_per_block", (256, 128)),
+    ("steps_per_poll", (32, 16, 64)),
+    ("persistent", (0, 1)),
+    ("donate_reserve", (0, -1, 30000)),
+    ("frontier_target", (2048, 1024, 4096)),
+)
+
+
+def autotune(solver, tiles, space=AUTOTUNE_SPACE, reps=2, clock=None, log=None):
+    """Pick the fastest launch and balance settings for a workload.
+
+    Coordinate descent over `space` (parameter, candidate values), starting
+    from the solver's current settings; each candidate is timed as the best
+    of `reps` host-buffer solves after one untimed solve.  These settings
+    change only speed: every candidate must return the same lengths and
+    per-iteration node counts, and a candidate that does not raises.  The
+    solver is left with the best settings; returns (best settings dict,
+    [(settings, seconds), ...]).
+    """
+    import time
+    clock = clock or time.perf_counter
+    a = _as_tiles(tiles, solver.width)
+    cur = {f: int(getattr(solver.config, f)) for f, _ in SpConfig._fields_}
+    want = None
+    tried = {}
+
+    def measure(cfg):
+        key = tuple(sorted(cfg.items()))
+        if key in tried:
+            return tried[key]
+        solver.set_config(**cfg)
+        solver.solve_raw(a)
+        best, got = None, None
+        for _ in range(max(1, reps)):
+            t0 = clock()
+            res = solver.solve_raw(a)
+            dt = clock() - t0
+            if best is None or dt < best:
+                best = dt
+            got = [(int(r.status), int(r.len), tuple(int(x) for x in r.nodes[:r.n_iter])) for r in res[:a.shape[0]]]
+        nonlocal want
+        if want is None:
+            want = got
+        elif got != want:
+            raise RuntimeError("autotune: results changed under %s" % (cfg,))
+        tried[key] = best
+        if log:
+            log("%s: %.2f ms" % (cfg, best * 1e3))
+        return best
+
+    best_t = measure(dict(cur))
+    for name, values in space:
+        for v in values:
+            if v == cur[name]:
+                continue
+            cand = dict(cur, **{name: v})
+            t = measure(cand)
+            if t < best_t:
+                best_t, cur = t, cand
+    solver.set_config(**cur)
+    history = [(dict(k), t) for k, t in tried.items()]
+    return cur, history
+
+
 def gemm_bf16_nt(a_bits, b_bits):
     """C = A . B^T on the tensor cores; A [m][k], B [256][k] as bf16 bit patterns (uint16)."""
     lib = load()
