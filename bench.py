@@ -102,6 +102,20 @@ def dist_setup():
     return world, rank, local
 
 
+def job_max_sum(max_vals, sum_vals, world, device):
+    """Whole-job figures: the max over ranks of each of `max_vals` (times)
+    and the sum over ranks of each of `sum_vals` (work).  One rank: as is."""
+    if world <= 1:
+        return [float(x) for x in max_vals], [float(x) for x in sum_vals]
+    import torch
+    import torch.distributed as dist
+    tm = torch.tensor([float(x) for x in max_vals], dtype=torch.float64, device=device)
+    ts = torch.tensor([float(x) for x in sum_vals], dtype=torch.float64, device=device)
+    dist.all_reduce(tm, op=dist.ReduceOp.MAX)
+    dist.all_reduce(ts, op=dist.ReduceOp.SUM)
+    return tm.tolist(), ts.tolist()
+
+
 def workload(rank, n=100):
     import instances
     return 4, instances.random_permutations(4, n, seed=0x15B + rank)
@@ -378,14 +392,7 @@ def main():
                 raise RuntimeError("lengths changed between steps")
             nodes += sum(res[i].nodes_total for i in range(n))
     total_ms = sum(step_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        tn = torch.tensor([nodes], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(tn)
-        total_ms, all_nodes = float(t.item()), float(tn.item())
-    else:
-        all_nodes = float(nodes)
+    (total_ms,), (all_nodes,) = job_max_sum([total_ms], [nodes], world, "cuda")
     value = all_nodes / (total_ms / 1000.0)
 
     # e2e: host buffers through sp_solve_batch (H2D/D2H inside)
@@ -405,10 +412,7 @@ def main():
         if [res[i].len for i in range(n)] != ref_lens:
             raise RuntimeError("e2e lengths differ")
     e2e_total = sum(e2e_ms)
-    if world > 1:
-        t = torch.tensor([e2e_total], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_total = float(t.item())
+    (e2e_total,), _ = job_max_sum([e2e_total], [], world, "cuda")
     e2e_value = all_nodes / (e2e_total / 1000.0)
 
     peak, peak_kind = load_peaks()
