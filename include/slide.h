@@ -224,6 +224,14 @@ int sp_lbm_gradients(sp_solver *s, const uint8_t *tiles, const int32_t *slack, c
  * 64): the model's GEMM on its own, for testing. */
 int sp_gemm_bf16_nt(const uint16_t *a, const uint16_t *b, float *c, int m, int n, int k);
 
+/* Self-test of the bounded device waits (no counterpart in the reference,
+ * whose kernels have no waits): runs the search kernel on a pool that
+ * reports one queued task that is never published, so every lane waits for
+ * it.  The kernel must give up after timeout_ms (100..60000) of no progress
+ * and report SP_ERR_TIMEOUT in *device_status without faulting; the solver
+ * stays usable.  Returns SP_OK when the launch itself worked. */
+int sp_selftest_stall(sp_solver *s, int timeout_ms, int32_t *device_status);
+
 int sp_last_stats(const sp_solver *s, sp_stats *out);
 const char *sp_status_string(int status);
 const char *sp_last_error(const sp_solver *s);

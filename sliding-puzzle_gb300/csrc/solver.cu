@@ -1502,6 +1502,54 @@ int sp_dfs_round(sp_solver *s, const uint8_t *roots, const int32_t *depth, const
   return SP_OK;
 }
 
+int sp_selftest_stall(sp_solver *s, int timeout_ms, int32_t *device_status) {
+  if (!s || !device_status || timeout_ms < 100 || timeout_ms > 60000) return SP_ERR_ARG;
+  *device_status = SP_OK;
+  int rc = ensure_pool(s, 1);
+  if (rc) return rc;
+  if ((rc = ensure(s, &s->d_subs, &s->subs_cap, 1)) || (rc = ensure(s, &s->d_sub_nodes, &s->sub_nodes_cap, 1)))
+    return rc;
+  if (!s->d_limit || s->inst_cap < 1) {
+    SP_CUDA(s, cudaMalloc(&s->d_limit, 64 * sizeof(int32_t)));
+    SP_CUDA(s, cudaMalloc(&s->d_sol, 64 * sizeof(Solution)));
+    s->inst_cap = 64;
+  }
+  // an empty pool, then one task counted as queued at index 0 that no
+  // producer ever publishes: every lane that claims it waits for it
+  SP_CUDA(s, launch_pool_init(s->d_tasks, nullptr, nullptr, nullptr, 0, s->d_seq, s->cap, s->d_ctl, s->st));
+  SP_CUDA(s, s->h_cnt.reserve(4));
+  s->h_cnt.p[0] = 1;
+  SP_CUDA(s, cudaMemcpyAsync(&s->d_ctl->tail, s->h_cnt.p, sizeof(uint32_t), cudaMemcpyHostToDevice, s->st));
+  SP_CUDA(s, cudaMemcpyAsync(&s->d_ctl->outstanding, s->h_cnt.p, sizeof(uint32_t), cudaMemcpyHostToDevice, s->st));
+  RoundParams P{};
+  P.subs = s->d_subs;
+  P.tasks = s->d_tasks;
+  P.seq = s->d_seq;
+  P.cap = s->cap;
+  P.ctl = s->d_ctl;
+  P.inst_limit = s->d_limit;
+  P.sub_nodes = s->d_sub_nodes;
+  P.sol = s->d_sol;
+  P.ht = s->d_ht;
+  P.pdb = s->d_pdb;
+  P.min_slack = s->cfg.donate_min_slack;
+  P.steps = s->cfg.steps_per_poll;
+  P.donate = 1;
+  P.timeout_ns = (unsigned long long)timeout_ms * 1000000ull;
+  P.poll_ns = 2000;
+  P.reserve = 0;
+  P.spread = 1;
+  int grid = 0;
+  const int block = s->cfg.threads_per_block == 128 ? 128 : 256;
+  SP_CUDA(s, launch_search_round(s->w, s->heur == SP_HEUR_PDB, block, s->cfg.blocks_per_sm, s->num_sms, P, s->st,
+                                 &grid));
+  SP_CUDA(s, s->h_ctl.reserve(1));
+  SP_CUDA(s, cudaMemcpyAsync(s->h_ctl.p, s->d_ctl, sizeof(PoolCtl), cudaMemcpyDeviceToHost, s->st));
+  SP_CUDA(s, cudaStreamSynchronize(s->st));
+  *device_status = s->h_ctl.p->error;
+  return SP_OK;
+}
+
 uint64_t sp_lbm_num_params(int width) {
   return (width == 4 || width == 5) ? (uint64_t)lbm::num_params(width) : 0;
 }

@@ -105,6 +105,7 @@ def load(build=True):
         "sp_lbm_train_step": (I32, [P, P, P, P, I32, ctypes.c_float, P]),
         "sp_lbm_gradients": (I32, [P, P, P, P, I32, P, P]),
         "sp_gemm_bf16_nt": (I32, [P, P, P, I32, I32, I32]),
+        "sp_selftest_stall": (I32, [P, I32, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -233,6 +234,13 @@ class Solver:
         self._check(self.lib.sp_dfs_round(self.h, a.ctypes.data, d.ctypes.data, p.ctypes.data, n, int(limit),
                                           nodes.ctypes.data, ctypes.byref(found)), "sp_dfs_round")
         return nodes, int(found.value)
+
+    def selftest_stall(self, timeout_ms=200):
+        """Device status of a search launch whose only task never arrives
+        (SP_ERR_TIMEOUT = -8 when the bounded waits work)."""
+        st = ctypes.c_int32(0)
+        self._check(self.lib.sp_selftest_stall(self.h, int(timeout_ms), ctypes.byref(st)), "sp_selftest_stall")
+        return int(st.value)
 
     # --- learned load balancer ---
     def lbm_num_params(self):

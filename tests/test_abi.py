@@ -68,6 +68,9 @@ def test_rejects_bad_arguments_without_gpu():
     assert lib.sp_create(6, 0, None, ctypes.byref(h)) == -1
     assert lib.sp_create(4, 7, None, ctypes.byref(h)) == -1
     assert lib.sp_solve_batch(None, None, 0, None) == -1
+    st = ctypes.c_int32(0)
+    assert lib.sp_selftest_stall(None, 200, ctypes.byref(st)) == -1
+    assert lib.sp_lbm_num_params(6) == 0 and lib.sp_lbm_num_params(5) > lib.sp_lbm_num_params(4)
 
 
 def test_no_cpu_fallback_when_no_gpu():
