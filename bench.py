@@ -241,18 +241,19 @@ def run_workload(args):
     import slide
     torch.cuda.set_device(0)
     out = []
-    modes = [("round", 0), ("persistent", 1)]
+    modes = [("round", dict(persistent=0)), ("persistent", dict(persistent=1, handback_nodes=0)),
+             ("hybrid", dict(persistent=1, handback_nodes=100000))]
     if args.workload == "15_md_walk60":
         w, states = instances.config_instances("15_md_walk60")
         for name, pers in modes:
-            s = slide.Solver(w, "manhattan", lb_mode="static", persistent=pers)
+            s = slide.Solver(w, "manhattan", lb_mode="static", **pers)
             dt, res, st = _timed_solve(s, states, reps=3)
             out.append(_summary("15_md_walk60/" + name, dt, res, st, {"heuristic": "manhattan"}))
             s.close()
     elif args.workload == "15_mixed4096":
         w, states = instances.config_instances("15_mixed4096")
         for name, pers in modes:
-            s = slide.Solver(w, "pdb", lb_mode="static", persistent=pers, frontier_target=args.frontier)
+            s = slide.Solver(w, "pdb", lb_mode="static", frontier_target=args.frontier, **pers)
             s.build_pdb()
             dt, res, st = _timed_solve(s, states, reps=2)
             out.append(_summary("15_mixed4096/" + name, dt, res, st,
@@ -318,7 +319,11 @@ def main():
     ap.add_argument("--instances", type=int, default=100)
     ap.add_argument("--frontier", type=int, default=2048)
     ap.add_argument("--lb", default="static")
-    ap.add_argument("--persistent", type=int, default=0, choices=[0, 1])
+    ap.add_argument("--persistent", type=int, default=None, choices=[0, 1],
+                    help="threshold loop on the device (default: the library's, 1)")
+    ap.add_argument("--handback", type=int, default=None,
+                    help="persistent mode: nodes per instance iteration from which the host round loop takes over "
+                         "(default: the library's, 100000; 0 = never)")
     ap.add_argument("--autotune", action="store_true",
                     help="pick block size, poll interval, persistence and donation reserve first "
                          "(the root-set size stays the configured one)")
@@ -343,7 +348,12 @@ def main():
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     w, states = workload(rank, args.instances)
     n = states.shape[0]
-    solver = slide.Solver(w, "pdb", frontier_target=args.frontier, lb_mode=args.lb, persistent=args.persistent)
+    opts = dict(frontier_target=args.frontier, lb_mode=args.lb)
+    if args.persistent is not None:
+        opts["persistent"] = args.persistent
+    if args.handback is not None:
+        opts["handback_nodes"] = args.handback
+    solver = slide.Solver(w, "pdb", **opts)
     t0 = time.perf_counter()
     solver.build_pdb()
     pdb_ms = 1000 * (time.perf_counter() - t0)
@@ -436,10 +446,12 @@ def main():
             "config": {"workload": "15puzzle_random100_pdb555", "instances_per_gpu": n,
                        "heuristic": "additive 5-5-5 PDB, max(regular, reflected)",
                        "frontier_target": args.frontier, "lb": args.lb + "+donation",
-                       "threshold_loop": ("device (one launch)" if (tuned or {}).get("persistent", args.persistent)
-                                          else "host (one launch per round)"),
+                       "threshold_loop": (("device, handing iterations of >= %d nodes per instance to the "
+                                           "host round loop" % solver.config.handback_nodes
+                                           if solver.config.handback_nodes else "device (one launch)")
+                                          if solver.config.persistent else "host (one launch per round)"),
                        "autotuned": {k: tuned[k] for k in ("threads_per_block", "steps_per_poll", "persistent",
-                                                           "donate_reserve")} if tuned else None,
+                                                           "handback_nodes", "donate_reserve")} if tuned else None,
                        "parallelism": "replicas" if world > 1 else "1 GPU",
                        "l2": "512 MB buffer written between timed steps",
                        "pdb_build_ms": round(pdb_ms, 2)},

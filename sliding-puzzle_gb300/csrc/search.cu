@@ -175,6 +175,16 @@ __device__ __noinline__ void warp_advance(const RoundParams &P, uint32_t i, uint
     unsigned long long tot = 0;
     for (uint32_t q = lane; q < na; q += 32) tot += __ldcg(ld + q);
     for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
+    if (P.handback_nodes && tot >= P.handback_nodes) {
+      // a large iteration is next: the host round loop finishes this
+      // instance (its loads of iteration r - 1 stay in `ld`)
+      if (lane == 0) {
+        P.inst_final[i] = r - 1;
+        P.inst_fin_ns[i] = globaltimer();
+        P.inst_status[i] = kStatusHandback;
+      }
+      return;
+    }
     const double avg = (double)tot / (double)na;
     for (uint32_t q = lane; q < ns; q += 32) nx[q] = 0;
     // longest first: bucket = binary exponent of load / average (0 = no load)

@@ -615,6 +615,7 @@ int launch_round(sp_solver *s, const RoundPlan &plan, size_t n_subs, size_t n_in
     P.t_begin_ns = m.t0_ns;
     P.n_subs = (uint32_t)n_subs;
     P.static_split = (s->cfg.lb_mode == SP_LB_STATIC_STEAL || s->cfg.lb_mode == SP_LB_LEARNED) ? 1 : 0;
+    P.handback_nodes = (unsigned long long)s->cfg.handback_nodes;
     SP_CUDA(s, launch_search_multi(s->w, s->heur == SP_HEUR_PDB, block, s->cfg.blocks_per_sm, s->num_sms, P,
                                    s->st, &grid));
   } else {
@@ -970,6 +971,7 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
   s->stats.d2h_bytes += ni * (8 + kMaxIters * 8);
   const Solution *sols = s->h_sols.p;
   int rounds = 0;
+  std::vector<unsigned long long> loads;
   for (size_t i = 0; i < ni; ++i) {
     Instance &I = inst[i];
     if (I.done) {
@@ -990,6 +992,31 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
     if (fin_ns[i] && fin_ns[i] >= t0[0]) R->seconds = pre_s + 1e-9 * (double)(fin_ns[i] - t0[0]);
     if (fin[i] < 0) {
       R->status = SP_ERR_TIMEOUT;
+    } else if (st[i] == kStatusHandback) {
+      // continue in the round loop from iteration fin + 1 with the loads the
+      // device measured in iteration fin
+      R->seconds = 0.0;
+      if (loads.empty()) {
+        loads.resize(2 * std::max<size_t>(n_subs, 1));
+        SP_CUDA(s, cudaMemcpy(loads.data(), m.loads, loads.size() * sizeof(unsigned long long),
+                              cudaMemcpyDeviceToHost));
+        s->stats.d2h_bytes += loads.size() * sizeof(unsigned long long);
+      }
+      const int f = fin[i];
+      const unsigned long long *lf = loads.data() + (size_t)(f & 1) * n_subs + I.sub_base;
+      uint64_t tot = 0;
+      for (size_t q = 0; q < I.leaves.size(); ++q) {
+        I.last_load[q] = lf[q];
+        tot += lf[q];
+      }
+      I.last_total = tot;
+      I.prev_total = 0;
+      if (f - 1 >= I.iter) {
+        const uint64_t all = itn[i * kMaxIters + (size_t)(f - 1)], in = interior_nodes(I, I.h0 + 2 * (f - 1));
+        I.prev_total = all > in ? all - in : 0;
+      }
+      I.iter = f + 1;
+      continue;
     } else if (st[i]) {
       R->status = st[i];
     } else {
@@ -1002,7 +1029,7 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
   s->stats.rounds = rounds;
   const double wall = ms_since(t_start);
   for (auto &I : inst)
-    if (I.out->seconds == 0.0) I.out->seconds = wall / 1000.0;
+    if (I.done && I.out->seconds == 0.0) I.out->seconds = wall / 1000.0;
   s->stats.wall_ms = wall;
   return SP_OK;
 }
@@ -1109,7 +1136,17 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
   }
   SP_CUDA(s, s->h_limits.reserve(inst.size()));
   s->stats.frontier_ms += ms_since(t_front);
-  if (s->cfg.persistent) return solve_multi(s, tiles, inst, n_subs, t_start);
+  // persistent mode: the device loop; instances it hands back (large
+  // iterations ahead) continue in the round loop below
+  int round0 = 0;
+  if (s->cfg.persistent) {
+    rc = solve_multi(s, tiles, inst, n_subs, t_start);
+    if (rc) return rc;
+    bool left = false;
+    for (auto &I : inst) left |= !I.done;
+    if (!left) return SP_OK;
+    round0 = 1;  // round statistics after the persistent launch's slot
+  }
 
   std::vector<int32_t> limits(inst.size(), 0);
   for (int round = 0; round < SP_MAX_ITERS; ++round) {
@@ -1117,7 +1154,7 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
     for (auto &I : inst) active += !I.done;
     if (!active) break;
     const auto t_round = std::chrono::steady_clock::now();
-    const int ri = std::min(round, SP_MAX_ROUNDS - 1);
+    const int ri = std::min(round + round0, SP_MAX_ROUNDS - 1);
     s->stats.round_instances[ri] = active;
     for (size_t i = 0; i < inst.size(); ++i) {
       limits[i] = inst[i].done ? -1 : inst[i].h0 + 2 * inst[i].iter;
@@ -1228,10 +1265,13 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
     s->stats.round_host_ms[ri] = (float)(ms_since(t_round) - s->stats.round_kernel_ms[ri]);
   }
   const double wall = ms_since(t_start);
+  int iters = 0;
   for (auto &I : inst) {
     if (I.out->seconds == 0.0) I.out->seconds = wall / 1000.0;
     if (!I.done && I.out->status == SP_OK) I.out->status = SP_ERR_LIMIT;
+    iters = std::max(iters, I.out->n_iter);
   }
+  if (round0) s->stats.rounds = iters;  // threshold iterations, as in persistent mode
   s->stats.wall_ms = wall;
   return SP_OK;
 }
@@ -1242,7 +1282,7 @@ bool config_ok(const sp_config *c) {
          c->lb_mode >= SP_LB_STEAL && c->lb_mode <= SP_LB_LEARNED && c->donate_min_slack >= 0 &&
          c->steps_per_poll >= 1 && c->steps_per_poll <= 4096 && c->timeout_ms >= 100 &&
          c->timeout_ms <= 600000 && c->static_split_cap >= 1 && c->donate_reserve >= -1 &&
-         (c->persistent == 0 || c->persistent == 1);
+         (c->persistent == 0 || c->persistent == 1) && c->handback_nodes >= 0;
 }
 
 }  // namespace
@@ -1260,7 +1300,8 @@ void sp_config_default(sp_config *c) {
   c->timeout_ms = 20000;
   c->static_split_cap = 10;
   c->donate_reserve = 0;
-  c->persistent = 0;
+  c->persistent = 1;            // device loop for the small iterations,
+  c->handback_nodes = 100000;   // round loop from ~1e5 nodes per instance iteration
 }
 
 int sp_create(int width, int heuristic, const sp_config *cfg, sp_solver **out) {

@@ -16,6 +16,9 @@ constexpr int kMaxIters = 96;                // threshold iterations per instanc
 constexpr int kPathWords = 10;               // 2-bit moves: 160 moves per record
 constexpr int kMaxPath = kPathWords * 16;
 constexpr uint8_t kNoPre = 0xFF;
+// Per-instance device status (besides sp_status codes): the instance left the
+// persistent loop for the host round loop after a completed iteration.
+constexpr int32_t kStatusHandback = 1;
 
 // Blank displacement of move d (0 up, 1 right, 2 left, 3 down).
 SP_HD int move_delta(int w, int d) { return d == 0 ? -w : d == 1 ? 1 : d == 2 ? -1 : w; }

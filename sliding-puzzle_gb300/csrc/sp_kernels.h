@@ -49,6 +49,7 @@ struct RoundParams {
   unsigned long long *t_begin_ns;     // %globaltimer at the launch's first block start (atomicMin)
   uint32_t n_subs;
   int32_t static_split;
+  unsigned long long handback_nodes;  // 0: never hand an instance back to the host
 };
 
 // One threshold round: grid = num_sms * blocks_per_sm (0 = occupancy maximum).

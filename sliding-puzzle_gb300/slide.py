@@ -33,7 +33,8 @@ class SpConfig(ctypes.Structure):
                 ("blocks_per_sm", ctypes.c_int32), ("lb_mode", ctypes.c_int32),
                 ("donate_min_slack", ctypes.c_int32), ("steps_per_poll", ctypes.c_int32),
                 ("timeout_ms", ctypes.c_int32), ("static_split_cap", ctypes.c_int32),
-                ("donate_reserve", ctypes.c_int32), ("persistent", ctypes.c_int32)]
+                ("donate_reserve", ctypes.c_int32), ("persistent", ctypes.c_int32),
+                ("handback_nodes", ctypes.c_int32)]
 
 
 class SpResult(ctypes.Structure):
@@ -314,7 +315,8 @@ def result_dict(r):
 AUTOTUNE_SPACE = (
     ("threads_per_block", (256, 128)),
     ("steps_per_poll", (32, 16, 64)),
-    ("persistent", (0, 1)),
+    ("persistent", (1, 0)),
+    ("handback_nodes", (100000, 0, 30000, 1000000)),
     ("donate_reserve", (0, -1, 30000)),
     ("frontier_target", (2048, 1024, 4096)),
 )
