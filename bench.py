@@ -429,7 +429,9 @@ def main():
     kms = sum(kern_ms)
     achieved = nodes * BYTES_PER_NODE / (kms / 1000.0) / 1e9 if kms > 0 else 0.0
     traffic = None  # DRAM bytes per search launch, from the committed ncu summary
-    prof = os.path.join(ROOT, "profiles", "search_round_pdb15_random100.md")
+    hybrid = solver.config.persistent and solver.config.handback_nodes
+    prof = os.path.join(ROOT, "profiles", "search_hybrid_pdb15_random100.md" if hybrid
+                        else "search_round_pdb15_random100.md")
     if os.path.exists(prof):
         for line in open(prof):
             if line.startswith("traffic_bytes_per_launch:"):
