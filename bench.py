@@ -275,7 +275,9 @@ def run_workload(args):
         def log(m):
             print("[lb_ab %.1fs] %s" % (time.perf_counter() - t_start, m), file=sys.stderr, flush=True)
         t_start = time.perf_counter()
-        s = slide.Solver(5, "pdb", frontier_target=8192)
+        # round mode: the learned model stands in for the loads of roots that
+        # the previous round did not measure, which only the round loop plans
+        s = slide.Solver(5, "pdb", frontier_target=8192, persistent=0)
         s.build_pdb()
         t0 = time.perf_counter()
         tiles, slack, target, mean = train_lb.make_dataset(s, args.tuples, 7, 0x1B, log=log)
