@@ -506,99 +506,95 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
   };
 
   // One edge of the depth-first search: generate the next child of the
-  // current node, or backtrack.  Returns true when the task is exhausted.
+  // current node, or undo the move into the current node.  Both slide one
+  // tile into the blank's cell and update the pattern index the same way, so
+  // they share one code path (lanes of a warp at different points of their
+  // walks stay converged); only the child's table lookups, the f-test and
+  // the stack bookkeeping differ.  Returns true when the task is exhausted.
   auto step = [&]() -> bool {
     uint32_t cand = legal_moves(W, blank) & (0xFu << it);
     if (pre >= 0) cand &= ~(1u << (3 - pre));
     if (k == 0) cand &= mask0;
-    if (cand) {
-      const int d = __ffs(cand) - 1;
-      const int src = blank + move_delta(W, d);
-      const int t = tile_at(src);
-      ++cnt;
-      int nh;
-      uint32_t nhvr = hvr, nhvf = hvf;
-      Idx<W> nir = ir, nif = iff;
-      if (PDB) {
-        const int pr = s_pat[t], pf = s_pat[N + t];
-        nir.add(pr, (int32_t)(s_code[t * N + blank] - s_code[t * N + src]));
-        nif.add(pf, (int32_t)(s_code[N * N + t * N + blank] - s_code[N * N + t * N + src]));
+    const bool gen = cand != 0;
+    if (!gen && k == 0) return true;
+    int dm;  // the blank's move this step
+    if (gen) {
+      dm = __ffs(cand) - 1;
+    } else {
+      --k;
+      if ((k & 15) == 15) top = s_stack[k >> 4][tid];
+      dm = 3 - (int)((top >> (2 * (k & 15))) & 3u);  // the reverse of the move into level k + 1
+    }
+    const int from = blank + move_delta(W, dm);
+    const int t = tile_at(from);  // slides from `from` into the blank's cell
+    int nh;
+    uint32_t nhvr = hvr, nhvf = hvf;
+    Idx<W> nir = ir, nif = iff;
+    int pr = 0, pf = 0;
+    if (PDB) {
+      pr = s_pat[t];
+      pf = s_pat[N + t];
+      nir.add(pr, (int32_t)(s_code[t * N + blank] - s_code[t * N + from]));
+      nif.add(pf, (int32_t)(s_code[N * N + t * N + blank] - s_code[N * N + t * N + from]));
+      if (gen || k >= HSAVE) {
         nhvr = set_byte(hvr, pr, lookup(W == 5 ? (pr != 0) : pr, nir.get(pr)));
         nhvf = set_byte(hvf, pf, lookup(W == 5 ? (pf != 0) : pf, nif.get(pf)));
-        nh = (int)max(byte_sum(nhvr), byte_sum(nhvf));
       } else {
-        nh = h + s_mdd[(d * N + src) * N + t];
+        const uint32_t sv = s_hsave[k][tid];  // the values this level had before the descent
+        nhvr = set_byte(hvr, pr, sv & 0xFFu);
+        nhvf = set_byte(hvf, pf, sv >> 8);
       }
-      if (g + 1 + nh <= limit) {
-        if (k + 1 >= MAXLEV || plen + k + 1 > kMaxPath) {
-          set_error(SP_ERR_STACK_OVERFLOW, (uint32_t)(plen + k));
-          return true;
-        }
-        slide(t, src, blank);
-        blank = src;
-        ++g;
-        h = nh;
-        if (PDB) {
-          if (k < HSAVE) {
-            const int pr = s_pat[t], pf = s_pat[N + t];
-            s_hsave[k][tid] = (uint16_t)(((hvr >> (8 * pr)) & 0xFFu) | (((hvf >> (8 * pf)) & 0xFFu) << 8));
-          }
-          ir = nir;
-          iff = nif;
-          hvr = nhvr;
-          hvf = nhvf;
-        }
-        const int sh = 2 * (k & 15);
-        top = (top & ~(3u << sh)) | ((uint32_t)d << sh);
-        if ((k & 15) == 15) s_stack[k >> 4][tid] = top;
-        ++k;
-        if (k < 64) cut &= ~(1ull << k);
-        pre = d;
-        it = 0;
-        if (nh == 0) record_goal();
-        if (splitk && k == splitk) {
-          // split task: this node (already counted as generated) becomes a
-          // task of its own (published outside the step loop); the lane then
-          // steps back
-          emit_pending = true;
-          it = 4;
-        }
-      } else {
-        it = d + 1;
-      }
-      return false;
-    }
-    if (k == 0) return true;
-    --k;
-    if ((k & 15) == 15) top = s_stack[k >> 4][tid];
-    const int d = (int)((top >> (2 * (k & 15))) & 3u);
-    const int back = blank - move_delta(W, d);
-    const int t = tile_at(back);
-    // the tile returns from `back` to the blank's cell
-    if (PDB) {
-      const int pr = s_pat[t], pf = s_pat[N + t];
-      ir.add(pr, (int32_t)(s_code[t * N + blank] - s_code[t * N + back]));
-      iff.add(pf, (int32_t)(s_code[N * N + t * N + blank] - s_code[N * N + t * N + back]));
-      if (k < HSAVE) {
-        const uint32_t sv = s_hsave[k][tid];
-        hvr = set_byte(hvr, pr, sv & 0xFFu);
-        hvf = set_byte(hvf, pf, sv >> 8);
-      } else {
-        hvr = set_byte(hvr, pr, lookup(W == 5 ? (pr != 0) : pr, ir.get(pr)));
-        hvf = set_byte(hvf, pf, lookup(W == 5 ? (pf != 0) : pf, iff.get(pf)));
-      }
-      h = (int)max(byte_sum(hvr), byte_sum(hvf));
+      nh = (int)max(byte_sum(nhvr), byte_sum(nhvf));
     } else {
-      h -= s_mdd[(d * N + blank) * N + t];
+      nh = h + s_mdd[(dm * N + from) * N + t];
     }
-    slide(t, back, blank);
-    blank = back;
-    --g;
-    it = d + 1;
-    if (k < 64 && ((cut >> k) & 1ull)) it = 4;
-    if (k == 0) pre = rpre;
-    else if (k & 15) pre = (int)((top >> (2 * ((k - 1) & 15))) & 3u);
-    else pre = (int)((s_stack[(k - 1) >> 4][tid] >> 30) & 3u);
+    if (gen) {
+      ++cnt;
+      if (g + 1 + nh > limit) {  // generated, not entered
+        it = dm + 1;
+        return false;
+      }
+      if (k + 1 >= MAXLEV || plen + k + 1 > kMaxPath) {
+        set_error(SP_ERR_STACK_OVERFLOW, (uint32_t)(plen + k));
+        return true;
+      }
+      if (PDB && k < HSAVE)
+        s_hsave[k][tid] = (uint16_t)(((hvr >> (8 * pr)) & 0xFFu) | (((hvf >> (8 * pf)) & 0xFFu) << 8));
+    }
+    slide(t, from, blank);
+    blank = from;
+    h = nh;
+    if (PDB) {
+      ir = nir;
+      iff = nif;
+      hvr = nhvr;
+      hvf = nhvf;
+    }
+    if (gen) {
+      ++g;
+      const int sh = 2 * (k & 15);
+      top = (top & ~(3u << sh)) | ((uint32_t)dm << sh);
+      if ((k & 15) == 15) s_stack[k >> 4][tid] = top;
+      ++k;
+      if (k < 64) cut &= ~(1ull << k);
+      pre = dm;
+      it = 0;
+      if (nh == 0) record_goal();
+      if (splitk && k == splitk) {
+        // split task: this node (already counted as generated) becomes a
+        // task of its own (published outside the step loop); the lane then
+        // steps back
+        emit_pending = true;
+        it = 4;
+      }
+    } else {
+      --g;
+      it = (3 - dm) + 1;  // the next sibling of the undone move
+      if (k < 64 && ((cut >> k) & 1ull)) it = 4;
+      if (k == 0) pre = rpre;
+      else if (k & 15) pre = (int)((top >> (2 * ((k - 1) & 15))) & 3u);
+      else pre = (int)((s_stack[(k - 1) >> 4][tid] >> 30) & 3u);
+    }
     return false;
   };
 
