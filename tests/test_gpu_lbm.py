@@ -132,3 +132,17 @@ def test_learned_lb_needs_a_model():
     with pytest.raises(slide.SlideError):
         s.solve(instances.random_walks(4, 2, 20, seed=1))
     s.close()
+
+
+def test_trained_model_beats_the_slack_only_estimate(gpu_solver):
+    """End to end through train_lb: labels from sp_dfs_round, GPU training,
+    held-out evaluation.  The model's squared error on log2 subtree sizes
+    must beat the best estimate that uses the slack alone (the mean per
+    slack value), and rank roots well: the ordering the balancer needs."""
+    import train_lb
+    s = gpu_solver(4, "pdb")
+    s.lbm_init(seed=3)
+    tiles, slack, target, _ = train_lb.make_dataset(s, 40000, 5, 0x51, node_budget=2e9, log=lambda m: None)
+    m = train_lb.train(s, tiles, slack, target, epochs=6, batch=2048, lr=2e-3, log=lambda m: None)
+    assert m["mse"] < 0.9 * m["slack_only_mse"], m
+    assert m["spearman"] > 0.6, m
