@@ -4,8 +4,9 @@ Workload (one step = solving the whole batch, every threshold iteration):
   15-puzzle, 100 uniformly random solvable permutations (seeded Fisher-Yates,
   parity-fixed), additive 5-5-5 PDB (max of regular and reflected partition),
   root set ~2048 subproblems per instance, static re-split + in-kernel
-  donation.  Rank r solves its own batch (seed + r): weak scaling, no data
-  collective.
+  donation, the library's default threshold loop (small iterations in one
+  persistent launch, large ones in the host round loop).  Rank r solves its
+  own batch (seed + r): weak scaling, no data collective.
 
 Prints one JSON line (rank 0).  `value` = generated nodes per second with
 the instances already in device memory (sp_solve_batch_device); `e2e` = the
@@ -242,7 +243,7 @@ def run_workload(args):
     torch.cuda.set_device(0)
     out = []
     modes = [("round", dict(persistent=0)), ("persistent", dict(persistent=1, handback_nodes=0)),
-             ("hybrid", dict(persistent=1, handback_nodes=100000))]
+             ("hybrid", dict(persistent=1, handback_nodes=600000))]
     if args.workload == "15_md_walk60":
         w, states = instances.config_instances("15_md_walk60")
         for name, pers in modes:
@@ -325,7 +326,7 @@ def main():
                     help="threshold loop on the device (default: the library's, 1)")
     ap.add_argument("--handback", type=int, default=None,
                     help="persistent mode: nodes per instance iteration from which the host round loop takes over "
-                         "(default: the library's, 100000; 0 = never)")
+                         "(default: the library's, 600000; 0 = never)")
     ap.add_argument("--autotune", action="store_true",
                     help="pick block size, poll interval, persistence and donation reserve first "
                          "(the root-set size stays the configured one)")
@@ -450,8 +451,8 @@ def main():
             "config": {"workload": "15puzzle_random100_pdb555", "instances_per_gpu": n,
                        "heuristic": "additive 5-5-5 PDB, max(regular, reflected)",
                        "frontier_target": args.frontier, "lb": args.lb + "+donation",
-                       "threshold_loop": (("device, handing iterations of >= %d nodes per instance to the "
-                                           "host round loop" % solver.config.handback_nodes
+                       "threshold_loop": (("device, handing iterations predicted at >= %d nodes per "
+                                           "instance to the host round loop" % solver.config.handback_nodes
                                            if solver.config.handback_nodes else "device (one launch)")
                                           if solver.config.persistent else "host (one launch per round)"),
                        "autotuned": {k: tuned[k] for k in ("threads_per_block", "steps_per_poll", "persistent",

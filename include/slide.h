@@ -84,9 +84,10 @@ typedef struct {
                                 0 = resident lanes / 16, -1 = only when a lane waits */
   int32_t persistent;        /* 1: every instance's threshold loop runs on the device in
                                 one launch; 0: one launch per threshold round */
-  int32_t handback_nodes;    /* persistent mode: an instance whose iteration generated at
-                                least this many nodes below its roots leaves the device
-                                loop and finishes in the round loop (0 = never) */
+  int32_t handback_nodes;    /* persistent mode: an instance whose next iteration is
+                                predicted (last iteration's nodes below its roots x its
+                                growth) at this many nodes or more leaves the device loop
+                                and finishes in the round loop (0 = never) */
 } sp_config;
 
 /* One instance's answer: "state in, optimal move sequence and per-iteration

@@ -175,7 +175,13 @@ __device__ __noinline__ void warp_advance(const RoundParams &P, uint32_t i, uint
     unsigned long long tot = 0;
     for (uint32_t q = lane; q < na; q += 32) tot += __ldcg(ld + q);
     for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(FULL, tot, o);
-    if (P.handback_nodes && tot >= P.handback_nodes) {
+    // the next iteration's size: this one's times the instance's growth
+    double grow = 6.0;
+    if (r >= 2) {
+      const unsigned long long prev = __ldcg(&P.iter_nodes[(size_t)i * kMaxIters + (r - 2)]);
+      if (prev) grow = fmin(30.0, fmax(2.0, (double)tot / (double)prev));
+    }
+    if (P.handback_nodes && (double)tot * grow >= (double)P.handback_nodes) {
       // a large iteration is next: the host round loop finishes this
       // instance (its loads of iteration r - 1 stay in `ld`)
       if (lane == 0) {

@@ -1301,7 +1301,7 @@ void sp_config_default(sp_config *c) {
   c->static_split_cap = 10;
   c->donate_reserve = 0;
   c->persistent = 1;            // device loop for the small iterations,
-  c->handback_nodes = 100000;   // round loop from ~1e5 nodes per instance iteration
+  c->handback_nodes = 600000;   // round loop from ~6e5 predicted nodes per instance iteration
 }
 
 int sp_create(int width, int heuristic, const sp_config *cfg, sp_solver **out) {

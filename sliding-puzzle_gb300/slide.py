@@ -316,7 +316,7 @@ AUTOTUNE_SPACE = (
     ("threads_per_block", (256, 128)),
     ("steps_per_poll", (32, 16, 64)),
     ("persistent", (1, 0)),
-    ("handback_nodes", (100000, 0, 30000, 1000000)),
+    ("handback_nodes", (600000, 0, 100000, 3000000)),
     ("donate_reserve", (0, -1, 30000)),
     ("frontier_target", (2048, 1024, 4096)),
 )
