@@ -259,6 +259,11 @@ __device__ __noinline__ void warp_advance(const RoundParams &P, uint32_t i, uint
 // Resident threads per SM the search kernels are compiled for (the register
 // budget: 768 threads leave 80 registers a thread; 24 warps per SM hide the
 // pattern-table latency markedly better than 16).
+// Longest sleep of a warp with no lane searching between pool polls (ns).
+#ifndef SP_MAX_BACKOFF_NS
+#define SP_MAX_BACKOFF_NS 16384
+#endif
+
 #ifndef SP_SEARCH_THREADS_PER_SM
 #define SP_SEARCH_THREADS_PER_SM 768
 #endif
@@ -633,7 +638,7 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
 
   unsigned long long last_change = 0;
   uint32_t last_out = 0xFFFFFFFFu, last_tail = 0xFFFFFFFFu, last_hb = 0xFFFFFFFFu, beat = 0;
-  unsigned backoff = 256;  // idle-warp sleep, ns, doubled up to 32 us
+  unsigned backoff = 256;  // idle-warp sleep, ns, doubled up to SP_MAX_BACKOFF_NS
   unsigned long long c_steps = 0, c_slots = 0, c_idle = 0;
   const long long t_begin = clock64();
 
@@ -725,7 +730,7 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
         }
       }
       __nanosleep(backoff);
-      backoff = min(backoff * 2u, 16384u);
+      backoff = min(backoff * 2u, (unsigned)SP_MAX_BACKOFF_NS);
       c_idle += (unsigned long long)(clock64() - t_iter);
       continue;
     }

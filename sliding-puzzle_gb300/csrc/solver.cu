@@ -43,6 +43,12 @@
 #include "sp_defs.h"
 #include "sp_kernels.h"
 
+// Shortest interval between two reads of the pool's control words by one
+// block (ns); the block shares what it read.
+#ifndef SP_POLL_NS
+#define SP_POLL_NS 2000
+#endif
+
 namespace sp {
 
 static std::atomic<uint64_t> g_launches{0};
@@ -588,7 +594,7 @@ int launch_round(sp_solver *s, const RoundPlan &plan, size_t n_subs, size_t n_in
   P.steps = s->cfg.steps_per_poll;
   P.donate = s->cfg.lb_mode == SP_LB_NONE ? 0 : 1;
   P.timeout_ns = (unsigned long long)s->cfg.timeout_ms * 1000000ull;
-  P.poll_ns = 2000;
+  P.poll_ns = SP_POLL_NS;
   const int block = s->cfg.threads_per_block == 128 ? 128 : 256;
   const uint32_t lanes = (uint32_t)(s->last_lanes > 0 ? s->last_lanes : s->num_sms * 1024);
   P.reserve = s->cfg.donate_reserve < 0 ? 0u : s->cfg.donate_reserve > 0 ? (uint32_t)s->cfg.donate_reserve
@@ -1577,7 +1583,7 @@ int sp_selftest_stall(sp_solver *s, int timeout_ms, int32_t *device_status) {
   P.steps = s->cfg.steps_per_poll;
   P.donate = 1;
   P.timeout_ns = (unsigned long long)timeout_ms * 1000000ull;
-  P.poll_ns = 2000;
+  P.poll_ns = SP_POLL_NS;
   P.reserve = 0;
   P.spread = 1;
   int grid = 0;
