@@ -326,6 +326,7 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
   int rblank = 0, rpre = -1, groot = 0, plen = 0;
   uint32_t mask0 = 0, top = 0, sub = 0;
   uint64_t cut = 0;
+  uint32_t lo = 0;  // donation walk cache: level | blank << 8 | (incoming move + 1) << 16
   unsigned long long cnt = 0;
   Idx<W> ir, iff;
   uint32_t hvr = 0, hvf = 0;
@@ -497,6 +498,7 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
     rblank = blank;
     rpre = pre;
     groot = g;
+    lo = ((uint32_t)rblank << 8) | ((uint32_t)(rpre + 1) << 16);
     k = 0;
     it = 0;
     top = 0;
@@ -612,28 +614,34 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
   // Give the untried moves of the shallowest open level (slack >= min_slack)
   // to a waiting lane.  Returns the level donated, or -1.
   auto find_donation = [&](uint32_t &mask_out) -> int {
-    int bl = rblank, pr = rpre;
+    // resume at the first level not yet seen exhausted (`lo`): a level only
+    // loses untried moves during a task, so the walk never needs to look
+    // below it again; above the current depth the cache restarts at k
+    int j = (int)(lo & 0xFFu), bl = (int)((lo >> 8) & 0xFFu), pr = (int)((lo >> 16) & 7u) - 1;
+    if (k < j) {
+      j = k;
+      bl = blank;
+      pr = pre;
+    }
     const int lim = min(k, 63);
-    for (int j = 0; j <= lim; ++j) {
-      if (limit - (groot + j) < P.min_slack) return -1;
-      uint32_t un;
-      if (j == k) {
-        un = legal_moves(W, bl) & (0xFu << it);
-      } else {
-        const int dj = stack_dir(j);
-        un = legal_moves(W, bl) & (0xFu << (dj + 1)) & 0xFu;
-        bl += move_delta(W, dj);
-        if (pr >= 0) un &= ~(1u << (3 - pr));
-        if (j == 0) un &= mask0;
-        pr = dj;
-        if (!((cut >> j) & 1ull) && un) { mask_out = un; return j; }
-        continue;
-      }
+    int found = -1;
+    for (; j <= lim; ++j) {
+      if (limit - (groot + j) < P.min_slack) break;
+      const int dj = j == k ? 0 : stack_dir(j);
+      uint32_t un = legal_moves(W, bl) & (j == k ? (0xFu << it) : ((0xFu << (dj + 1)) & 0xFu));
       if (pr >= 0) un &= ~(1u << (3 - pr));
       if (j == 0) un &= mask0;
-      if (!((cut >> j) & 1ull) && un) { mask_out = un; return j; }
+      if (!((cut >> j) & 1ull) && un) {
+        mask_out = un;
+        found = j;
+        break;
+      }
+      if (j == k) break;
+      bl += move_delta(W, dj);
+      pr = dj;
     }
-    return -1;
+    lo = (uint32_t)min(j, 255) | ((uint32_t)bl << 8) | ((uint32_t)(pr + 1) << 16);
+    return found;
   };
 
   unsigned long long last_change = 0;
