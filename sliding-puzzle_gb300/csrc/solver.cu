@@ -122,7 +122,7 @@ struct Pinned {
     if (p) cudaFreeHost(p);
     p = nullptr;
     cap = 0;
-    size_t c = std::max<size_t>(n, 1024);
+    size_t c = std::max<size_t>({n, (size_t)1024, cap + cap / 2});  // geometric: pinned allocation is slow
     cudaError_t e = cudaMallocHost((void **)&p, c * sizeof(T));
     if (e == cudaSuccess) cap = c;
     return e;
@@ -187,6 +187,7 @@ struct sp_solver {
   size_t boards_cap = 0, h_cap = 0;
   // pinned staging
   Pinned<uint32_t> h_direct;
+  Pinned<Task> h_split;
   Pinned<unsigned long long> h_sub_nodes;
   Pinned<Solution> h_sols;
   Pinned<PoolCtl> h_ctl;
@@ -550,7 +551,9 @@ int launch_round(sp_solver *s, const RoundPlan &plan, size_t n_subs, size_t n_in
     if (rc) return rc;
     rc = ensure(s, &s->d_emit, &s->emit_cap, std::max<size_t>(plan.emit_bound, 1));
     if (rc) return rc;
-    SP_CUDA(s, cudaMemcpyAsync(s->d_split_a, plan.split.data(), plan.split.size() * sizeof(Task),
+    SP_CUDA(s, s->h_split.reserve(plan.split.size()));
+    memcpy(s->h_split.p, plan.split.data(), plan.split.size() * sizeof(Task));
+    SP_CUDA(s, cudaMemcpyAsync(s->d_split_a, s->h_split.p, plan.split.size() * sizeof(Task),
                                cudaMemcpyHostToDevice, s->st));
     s->stats.h2d_bytes += plan.split.size() * sizeof(Task);
   }
@@ -735,9 +738,8 @@ int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int3
   std::vector<uint8_t> bucket(nc, 127);
   const size_t nchunk = std::max<size_t>(1, std::min<size_t>(64, nc / 8192));
   auto chunk_lo = [&](size_t c) { return nc * c / nchunk; };
-  std::vector<size_t> need_c(nchunk, 0);
+  std::vector<size_t> kh(nchunk * 11, 0);  // per chunk: roots per split depth
   parallel_for(nchunk, [&](size_t c) {
-    size_t need = 0;
     for (size_t j = chunk_lo(c); j < chunk_lo(c + 1); ++j) {
       int e = -64;
       if (pred[j] > 0 && T > 0) {
@@ -747,24 +749,26 @@ int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int3
       bucket[j] = (uint8_t)(63 - e);
       if (T > 0 && pred[j] > T) {
         k[j] = (int8_t)std::max(0, std::min(e, std::min(kcap, (int)room[j] - 1)));
-        need += bound(k[j]);
+        ++kh[c * 11 + k[j]];
       }
     }
-    need_c[c] = need;
   });
-  size_t need = 0;
-  for (size_t x : need_c) need += x;
+  // piece budget: the deepest splits are cut first, i.e. every depth is
+  // capped at the largest cap whose pieces fit
+  size_t cnt_k[11] = {0};
+  for (size_t c = 0; c < nchunk; ++c)
+    for (int kk = 0; kk <= 10; ++kk) cnt_k[kk] += kh[c * 11 + kk];
   const size_t budget = (size_t)1 << 22;
-  while (need > budget) {  // trim the deepest splits first
-    int mk = 0;
-    for (int8_t kk : k) mk = std::max(mk, (int)kk);
-    if (!mk) break;
-    for (auto &kk : k)
-      if (kk == mk) {
-        need -= bound(kk) - bound(kk - 1);
-        --kk;
-      }
+  int kmax = 10;
+  for (; kmax > 0; --kmax) {
+    size_t need = 0;
+    for (int kk = 1; kk <= 10; ++kk) need += cnt_k[kk] * bound(std::min(kk, kmax));
+    if (need <= budget) break;
   }
+  if (kmax < 10)
+    parallel_for(nchunk, [&](size_t c) {
+      for (size_t j = chunk_lo(c); j < chunk_lo(c + 1); ++j) k[j] = (int8_t)std::min((int)k[j], kmax);
+    });
   // stable counting sort by bucket, split roots and whole roots separately:
   // per-chunk histograms, then every chunk scatters into its own ranges
   std::vector<uint32_t> hd(nchunk * 128, 0), hs(nchunk * 128, 0);
