@@ -259,6 +259,11 @@ __device__ __noinline__ void warp_advance(const RoundParams &P, uint32_t i, uint
 // Resident threads per SM the search kernels are compiled for (the register
 // budget: 768 threads leave 80 registers a thread; 24 warps per SM hide the
 // pattern-table latency markedly better than 16).
+// Most lanes of a warp that donate in one pass of its loop.
+#ifndef SP_MAX_DONORS
+#define SP_MAX_DONORS 8
+#endif
+
 // Longest sleep of a warp with no lane searching between pool polls (ns).
 #ifndef SP_MAX_BACKOFF_NS
 #define SP_MAX_BACKOFF_NS 16384
@@ -797,7 +802,7 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
       const unsigned key = lev >= 0 ? (unsigned)lev : 0xFFFFFFFFu;
       const unsigned best = __reduce_min_sync(FULL, key);
       const uint32_t shortfall = hd + P.reserve - tl;
-      const unsigned allowed = min(8u, 1u + shortfall / P.spread);
+      const unsigned allowed = min((unsigned)SP_MAX_DONORS, 1u + shortfall / P.spread);
       const unsigned cand = __ballot_sync(FULL, lev >= 0 && (unsigned)lev <= best + 1u);
       const unsigned rank = __popc(cand & ((1u << lane) - 1u));
       const bool donor = ((cand >> lane) & 1u) && rank < allowed && !(events & kDebt);
