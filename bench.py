@@ -171,26 +171,40 @@ def run_reference(args):
 
 
 def run_probe(args):
-    """Steady-state kernel probe: one root replicated `--roots` times in one
-    threshold round (identical subtrees, so no load imbalance)."""
+    """Steady-state kernel probes, one threshold round each.  balanced: one
+    root replicated `--roots` times (identical subtrees: no load imbalance,
+    every lane reads the same table entries).  mixed: `--roots` distinct walk
+    endpoints (100-220 moves for the 24-puzzle, 40-80 for the 15-puzzle),
+    each given the depth that puts it `--probe-slack`/2 threshold steps below
+    one common limit, so the table reads scatter as in a real search."""
     import torch
     import instances
     import slide
+    import train_lb
     torch.cuda.set_device(0)
     width = 4 if args.probe_width == 4 else 5
     s = slide.Solver(width, args.probe_heuristic)
     if args.probe_heuristic == "pdb":
         s.build_pdb()
-    root = instances.random_walks(width, 1, 50, seed=5)
-    h0 = int(s.heuristic_values(root)[0])
     n = args.roots
-    roots = np.repeat(root, n, axis=0)
-    zeros, pre = np.zeros(n, np.int32), -np.ones(n, np.int32)
-    s.dfs_round(roots[:1024], zeros[:1024], pre[:1024], h0 + args.probe_slack)  # warm-up
-    nodes, _ = s.dfs_round(roots, zeros, pre, h0 + args.probe_slack)
+    pre = -np.ones(n, np.int32)
+    if args.probe == "balanced":
+        root = instances.random_walks(width, 1, 50, seed=5)
+        h0 = int(s.heuristic_values(root)[0])
+        roots = np.repeat(root, n, axis=0)
+        depth = np.zeros(n, np.int32)
+        limit = h0 + args.probe_slack
+    else:
+        lo, hi = (100, 220) if width == 5 else (40, 80)
+        roots = train_lb.vector_walks(width, n, lo, hi, seed=7)
+        h = s.heuristic_values(roots).astype(np.int64)
+        limit = int(h.max()) + args.probe_slack
+        depth = (limit - args.probe_slack - h).astype(np.int32)
+    s.dfs_round(roots[:1024], depth[:1024], pre[:1024], limit)  # warm-up
+    nodes, _ = s.dfs_round(roots, depth, pre, limit)
     x = s.stats()
-    print(json.dumps({"probe": "balanced", "width": width, "heuristic": args.probe_heuristic, "roots": n,
-                      "nodes_per_root": int(nodes[0]), "kernel_ms": x["kernel_ms"],
+    print(json.dumps({"probe": args.probe, "width": width, "heuristic": args.probe_heuristic, "roots": n,
+                      "nodes_per_root": float(nodes.mean()), "kernel_ms": x["kernel_ms"],
                       "nodes_per_s": float(nodes.sum()) / (x["kernel_ms"] / 1000.0),
                       "lane_step_fraction": x["dev_lane_steps"] / max(1, x["dev_lane_slots"]),
                       "idle_fraction": x["dev_idle_cycles"] / max(1, x["dev_warp_cycles"])}), flush=True)
@@ -306,7 +320,7 @@ def run_workload(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--probe", choices=["balanced"], default=None)
+    ap.add_argument("--probe", choices=["balanced", "mixed"], default=None)
     ap.add_argument("--workload", choices=["15_md_walk60", "15_mixed4096", "24_bins", "lb_ab"], default=None)
     ap.add_argument("--tuples", type=int, default=1_000_000)
     ap.add_argument("--epochs", type=int, default=3)
