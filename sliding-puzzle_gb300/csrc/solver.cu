@@ -393,8 +393,12 @@ int finish_trees(sp_solver *s, std::vector<Instance> &inst) {
   std::vector<size_t> first(inst.size() + 1, 0);
   for (size_t i = 0; i < inst.size(); ++i) first[i + 1] = first[i] + inst[i].tree.size();
   parallel_for(inst.size(), [&](size_t i) {
-    size_t o = first[i];
-    for (auto &t : inst[i].tree) memcpy(boards.p + (o++) * s->n, t.board, (size_t)s->n);
+    uint8_t *o = boards.p + first[i] * s->n;
+    if (s->n == 16) {  // fixed sizes: the copies inline
+      for (auto &t : inst[i].tree) memcpy(o, t.board, 16), o += 16;
+    } else {
+      for (auto &t : inst[i].tree) memcpy(o, t.board, 25), o += 25;
+    }
   });
   SP_CUDA(s, cudaMemcpyAsync(s->d_boards, boards.p, total * s->n, cudaMemcpyHostToDevice, s->st));
   s->stats.h2d_bytes += total * s->n;
@@ -422,8 +426,24 @@ int finish_trees(sp_solver *s, std::vector<Instance> &inst) {
       else interior.push_back({t.maxf, t.nchild});
       if (t.h == 0) I.goals.push_back((int32_t)j);
     }
-    std::stable_sort(I.leaves.begin(), I.leaves.end(),
-                     [&](int32_t a, int32_t b) { return I.tree[(size_t)a].maxf < I.tree[(size_t)b].maxf; });
+    {  // stable counting sort of the leaves by maxf (a small range of integers)
+      int lo = INT32_MAX, hi = INT32_MIN;
+      for (int32_t x : I.leaves) {
+        lo = std::min(lo, I.tree[(size_t)x].maxf);
+        hi = std::max(hi, I.tree[(size_t)x].maxf);
+      }
+      if (!I.leaves.empty() && hi - lo < 4096) {
+        std::vector<uint32_t> cnt((size_t)(hi - lo) + 2, 0);
+        for (int32_t x : I.leaves) ++cnt[(size_t)(I.tree[(size_t)x].maxf - lo) + 1];
+        for (size_t b = 1; b < cnt.size(); ++b) cnt[b] += cnt[b - 1];
+        std::vector<int32_t> sorted(I.leaves.size());
+        for (int32_t x : I.leaves) sorted[cnt[(size_t)(I.tree[(size_t)x].maxf - lo)]++] = x;
+        I.leaves.swap(sorted);
+      } else {
+        std::stable_sort(I.leaves.begin(), I.leaves.end(),
+                         [&](int32_t a, int32_t b) { return I.tree[(size_t)a].maxf < I.tree[(size_t)b].maxf; });
+      }
+    }
     I.leaf_maxf.resize(I.leaves.size());
     I.leaf_g.resize(I.leaves.size());
     for (size_t q = 0; q < I.leaves.size(); ++q) {
