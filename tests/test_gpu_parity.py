@@ -203,3 +203,24 @@ def test_dfs_round_matches_subtree_counts(gpu_solver):
         if f >= 0 and (want_found < 0 or f < want_found):
             want_found = f
     assert found == want_found
+
+
+def test_korf100_all_lengths_pdb(gpu_solver):
+    """All 100 of test/result_15puzzle.txt's optimal lengths (korf100), 5-5-5 PDB."""
+    g = load_golden("korf100.json")["instances"]
+    states = np.array([x["tiles"] for x in g], dtype=np.uint8)
+    got = gpu_solver(4, "pdb").solve(states)
+    for x, a, t in zip(g, got, states):
+        assert a["status"] == 0 and a["len"] == x["len"], x["name"]
+        assert slide.is_solution(t, a["moves"], 4), x["name"]
+
+
+@pytest.mark.parametrize("heuristic", ["pdb", "manhattan"])
+def test_yama24_50_all_lengths(gpu_solver, heuristic):
+    """All of test/result_24puzzle.txt's yama24_50 optimal lengths."""
+    g = load_golden("yama24_50.json")["instances"]
+    states = np.array([x["tiles"] for x in g], dtype=np.uint8)
+    got = gpu_solver(5, heuristic).solve(states)
+    for x, a, t in zip(g, got, states):
+        assert a["status"] == 0 and a["len"] == x["len"], x["name"]
+        assert slide.is_solution(t, a["moves"], 5), x["name"]
