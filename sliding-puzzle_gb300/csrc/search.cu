@@ -598,10 +598,11 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
       pre = dm;
       it = 0;
       if (nh == 0) record_goal();
-      if (splitk && k == splitk) {
-        // split task: this node (already counted as generated) becomes a
-        // task of its own (published outside the step loop); the lane then
-        // steps back
+      if (splitk && k == 1) {
+        // split task with `splitk` levels left: this child (already counted
+        // as generated) becomes a task of its own with one level fewer
+        // (published outside the step loop), so a heavy root is split
+        // breadth-first by many lanes; the lane then steps back
         emit_pending = true;
         it = 4;
       }
@@ -777,7 +778,7 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
             D->sub = sub;
             D->plen = (uint16_t)len;
             D->mask = 0xF;
-            D->flags = 0;
+            D->flags = (uint8_t)(splitk - 1);
             for (int wi = 0; wi < kPathWords; ++wi) D->path[wi] = path_word(wi, len);
             st_release(&P.seq[t & (P.cap - 1u)], t + 1u);
             emitted = true;
