@@ -43,6 +43,14 @@
 #include "sp_defs.h"
 #include "sp_kernels.h"
 
+// Static split: a round's predicted work is cut into about this many pieces
+// per resident lane (the piece size T of plan_round).  Measured: 1 beats 4,
+// 16 and 64 (each piece costs a pre-pass expansion and a task start, and
+// donation evens out the rest) and 0.5 or less (more donations).
+#ifndef SP_SPLIT_PIECES_PER_LANE
+#define SP_SPLIT_PIECES_PER_LANE 1.0
+#endif
+
 // Shortest interval between two reads of the pool's control words by one
 // block (ns); the block shares what it read.
 #ifndef SP_POLL_NS
@@ -674,7 +682,8 @@ int launch_round(sp_solver *s, const RoundPlan &plan, size_t n_subs, size_t n_in
 
 // Static load balancing for the round: a root's work is predicted from its
 // previous round (load x the instance's growth per threshold step); a root
-// predicted above the round's piece size T is split ceil(log2(pred/T))
+// predicted above the round's piece size T (the round's predicted total
+// over SP_SPLIT_PIECES_PER_LANE pieces per resident lane) is split ceil(log2(pred/T))
 // levels by the device pre-pass -- the reference splits a root into
 // ceil(load/avg) pieces (src/24puzzle_block_parallel_with_pdb.cu:839-897) --
 // and whole roots are published in decreasing predicted size.  With the
@@ -747,7 +756,7 @@ int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int3
     }
   }
   const double lanes = s->last_lanes > 0 ? (double)s->last_lanes : (double)s->num_sms * 1024.0;
-  const double T = total / (lanes * 4.0);
+  const double T = total / (lanes * (double)SP_SPLIT_PIECES_PER_LANE);
   static const size_t pow3[12] = {1, 3, 9, 27, 81, 243, 729, 2187, 6561, 19683, 59049, 177147};
   auto bound = [&](int kk) { return kk ? 4 * pow3[kk - 1] : (size_t)0; };
   const int kcap = std::min(10, std::max(1, s->cfg.static_split_cap));
