@@ -16,10 +16,15 @@
 //    shared memory (src/15puzzle_block_parallel.cu:271-272 updates it with two
 //    constant-memory lookups);
 //  * PDB indices kept per pattern as mixed-radix integers and updated by one
-//    add per move, so a move costs one regular and one reflected table lookup
-//    instead of the reference's eight (src/24puzzle_block_parallel_with_pdb.cu
-//    :426-429); the idea of updating only the moved tile's pattern is Horie's
-//    (src_horie/idas_pdb.cu:221-254);
+//    add per move, so a generated child costs one regular and one reflected
+//    table lookup instead of the reference's eight
+//    (src/24puzzle_block_parallel_with_pdb.cu:426-429); the idea of updating
+//    only the moved tile's pattern is Horie's (src_horie/idas_pdb.cu:221-254);
+//    undoing a move restores the two overwritten pattern values from a
+//    per-level save in shared memory instead of looking them up again;
+//  * generating a child and undoing a move share one code path (both slide
+//    one tile into the blank), which keeps a warp's lanes converged while
+//    they are at different points of their walks;
 //  * load balance by a device task pool: lanes claim slots warp-aggregated
 //    (ballot + one atomicAdd per warp); claims may run ahead of the pool's
 //    tail, and while any lane waits, busy lanes donate the untried moves of
@@ -32,7 +37,9 @@
 // loop in one launch: the warp whose lane finishes an instance's last task of
 // an iteration publishes that instance's next iteration (warp_advance), so
 // instances never wait for each other and the host is not involved between
-// iterations.
+// iterations.  Its heavy roots go out as split tasks that expand one level
+// per claim (breadth-first across lanes); an instance whose next iteration
+// is predicted to be large is handed back to the host round loop.
 //
 // Every wait is bounded: a warp whose lanes all wait and see no change of the
 // pool for timeout_ns sets SP_ERR_TIMEOUT and every warp returns.  Nothing
