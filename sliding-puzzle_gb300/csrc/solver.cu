@@ -1,6 +1,14 @@
 // Host side of libslide: the C ABI (include/slide.h), the root-set
 // ("frontier") construction, the IDA* threshold-round loop and static load
-// balancing.  Device work is in search.cu and pdb_build.cu.
+// balancing.  Device work is in search.cu, pdb_build.cu and mlp.cu.
+//
+// A batch is solved in two phases by default: one persistent launch runs
+// every instance's small iterations on the device (solve_multi); an instance
+// whose next iteration is predicted large is handed back, with the per-root
+// loads the device measured, to the round loop (solve_impl), which plans
+// each round's static split on host worker threads (WorkPool) and launches
+// the split pre-pass and the search.  `persistent = 0` runs only the round
+// loop, `handback_nodes = 0` only the persistent launch.
 //
 // Reference counterparts:
 //   create_root_set       src/24puzzle_block_parallel_with_pdb.cu:454-490
