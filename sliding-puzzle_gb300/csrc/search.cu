@@ -119,6 +119,12 @@ __device__ __forceinline__ uint32_t set_byte(uint32_t v, int p, uint32_t x) {
 
 }  // namespace
 
+// Multi-iteration mode: split-piece load in units of the instance's average
+// root load (1, 2 and 4 measure alike).
+#ifndef SP_MULTI_PIECE
+#define SP_MULTI_PIECE 1.0
+#endif
+
 // Multi-iteration mode: the warp of the lane that finished an instance's last
 // task of an iteration completes that iteration (adds the root-set interior
 // count, checks for a goal) and publishes the next iteration's roots -- the
@@ -127,9 +133,6 @@ __device__ __forceinline__ uint32_t set_byte(uint32_t v, int p, uint32_t x) {
 // lanes of a warp with the same instance i; `hist` is the warp's 32 words of
 // shared memory.  Kept out of line: it is cold, and inlined its registers
 // would crowd the search loop.
-#ifndef SP_MULTI_PIECE
-#define SP_MULTI_PIECE 1.0  // split-piece load in units of the instance's average root load
-#endif
 __device__ __noinline__ void warp_advance(const RoundParams &P, uint32_t i, uint32_t *hist) {
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
