@@ -203,11 +203,14 @@ def run_probe(args):
     s.dfs_round(roots[:1024], depth[:1024], pre[:1024], limit)  # warm-up
     nodes, _ = s.dfs_round(roots, depth, pre, limit)
     x = s.stats()
-    print(json.dumps({"probe": args.probe, "width": width, "heuristic": args.probe_heuristic, "roots": n,
-                      "nodes_per_root": float(nodes.mean()), "kernel_ms": x["kernel_ms"],
-                      "nodes_per_s": float(nodes.sum()) / (x["kernel_ms"] / 1000.0),
-                      "lane_step_fraction": x["dev_lane_steps"] / max(1, x["dev_lane_slots"]),
-                      "idle_fraction": x["dev_idle_cycles"] / max(1, x["dev_warp_cycles"])}), flush=True)
+    d = {"probe": args.probe, "width": width, "heuristic": args.probe_heuristic, "roots": n,
+         "nodes_per_root": float(nodes.mean()), "kernel_ms": x["kernel_ms"],
+         "nodes_per_s": float(nodes.sum()) / (x["kernel_ms"] / 1000.0),
+         "lane_step_fraction": x["dev_lane_steps"] / max(1, x["dev_lane_slots"]),
+         "idle_fraction": x["dev_idle_cycles"] / max(1, x["dev_warp_cycles"])}
+    if args.probe_heuristic == "manhattan":
+        d["roofline"] = _int_roofline(float(nodes.sum()), x["kernel_ms"], slide.probe_int_issue()[0])
+    print(json.dumps(d), flush=True)
 
 
 def _timed_solve(solver, states, reps=1):
@@ -248,6 +251,18 @@ def _summary(label, dt, res, st, extra=None):
     return d
 
 
+def _int_roofline(nodes, kernel_ms, peak_ops):
+    """Integer-issue roofline of a Manhattan-heuristic search: the algorithmic
+    integer operations of its generated nodes over its kernel time, against
+    the integer rate sp_probe_int_issue measured in the same process."""
+    import slide
+    achieved = nodes * slide.MD_OPS_PER_NODE / (kernel_ms / 1000.0) / 1e9
+    peak = peak_ops / 1e9
+    return {"bound": "int-issue", "achieved": achieved, "peak": peak, "unit": "G int32 op/s",
+            "frac": achieved / peak, "ops_per_node": slide.MD_OPS_PER_NODE,
+            "peak_source": "sp_probe_int_issue, measured in this run"}
+
+
 def run_workload(args):
     """Secondary workloads (the other configurations of the benchmark plan),
     one JSON line each; the headline line is the default mode."""
@@ -260,10 +275,13 @@ def run_workload(args):
              ("hybrid", dict(persistent=1, handback_nodes=600000))]
     if args.workload == "15_md_walk60":
         w, states = instances.config_instances("15_md_walk60")
+        peak_ops, _ = slide.probe_int_issue()
         for name, pers in modes:
             s = slide.Solver(w, "manhattan", lb_mode="static", **pers)
             dt, res, st = _timed_solve(s, states, reps=3)
-            out.append(_summary("15_md_walk60/" + name, dt, res, st, {"heuristic": "manhattan"}))
+            d = _summary("15_md_walk60/" + name, dt, res, st, {"heuristic": "manhattan"})
+            d["roofline"] = _int_roofline(d["nodes"], st["kernel_ms"], peak_ops)
+            out.append(d)
             s.close()
     elif args.workload == "15_mixed4096":
         w, states = instances.config_instances("15_mixed4096")

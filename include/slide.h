@@ -236,6 +236,14 @@ int sp_gemm_bf16_nt(const uint16_t *a, const uint16_t *b, float *c, int m, int n
  * stays usable.  Returns SP_OK when the launch itself worked. */
 int sp_selftest_stall(sp_solver *s, int timeout_ms, int32_t *device_status);
 
+/* Measured 32-bit integer operation rate of the current device (lane
+ * operations per second; no counterpart in the reference): the roofline
+ * denominator of the Manhattan search, which is bound by integer issue.  One
+ * wave of resident blocks runs independent add/xor chains of `iters`
+ * (1..2^24) steps; the best of `reps` (1..100) timed launches is reported,
+ * its duration in *best_ms (may be NULL).  SP_ERR_CUDA without a GPU. */
+int sp_probe_int_issue(int32_t iters, int32_t reps, double *lane_ops_per_s, double *best_ms);
+
 int sp_last_stats(const sp_solver *s, sp_stats *out);
 const char *sp_status_string(int status);
 const char *sp_last_error(const sp_solver *s);

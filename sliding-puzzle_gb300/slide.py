@@ -107,6 +107,7 @@ def load(build=True):
         "sp_lbm_gradients": (I32, [P, P, P, P, I32, P, P]),
         "sp_gemm_bf16_nt": (I32, [P, P, P, I32, I32, I32]),
         "sp_selftest_stall": (I32, [P, I32, P]),
+        "sp_probe_int_issue": (I32, [I32, I32, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -394,6 +395,27 @@ def gemm_bf16_nt(a_bits, b_bits):
 
 def kernel_launch_count():
     return int(load().sp_kernel_launch_count())
+
+
+# Integer operations per generated node that the Manhattan search's
+# roofline charges, counted on the serial reference search
+# (src/24puzzle_expand.cc:111-143) plus the path push that returning a
+# solution needs: move legality 1, reverse-move test 1, node count 1, tile
+# read 1, blank swap 2, heuristic update 4 (two table reads, a subtraction,
+# an addition), goal test 1, f = g + h and its limit test 2, path push 1,
+# undo 2.
+MD_OPS_PER_NODE = 16
+
+
+def probe_int_issue(iters=1 << 16, reps=3):
+    """(lane operations per second, best launch ms) of the current device:
+    the integer-issue roofline denominator (sp_probe_int_issue)."""
+    lib = load()
+    rate, ms = ctypes.c_double(), ctypes.c_double()
+    st = lib.sp_probe_int_issue(int(iters), int(reps), ctypes.byref(rate), ctypes.byref(ms))
+    if st != 0:
+        raise SlideError(st, "sp_probe_int_issue failed: %s" % lib.sp_status_string(st).decode())
+    return rate.value, ms.value
 
 
 def replay(tiles, moves, width):

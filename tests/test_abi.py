@@ -71,6 +71,11 @@ def test_rejects_bad_arguments_without_gpu():
     st = ctypes.c_int32(0)
     assert lib.sp_selftest_stall(None, 200, ctypes.byref(st)) == -1
     assert lib.sp_lbm_num_params(6) == 0 and lib.sp_lbm_num_params(5) > lib.sp_lbm_num_params(4)
+    rate = ctypes.c_double(1.0)
+    assert lib.sp_probe_int_issue(1 << 16, 3, None, None) == -1
+    assert lib.sp_probe_int_issue(0, 3, ctypes.byref(rate), None) == -1
+    assert lib.sp_probe_int_issue((1 << 24) + 1, 3, ctypes.byref(rate), None) == -1
+    assert lib.sp_probe_int_issue(1 << 16, 0, ctypes.byref(rate), None) == -1
 
 
 def test_no_cpu_fallback_when_no_gpu():
@@ -81,3 +86,6 @@ def test_no_cpu_fallback_when_no_gpu():
     with pytest.raises(slide.SlideError) as e:
         slide.Solver(4, "manhattan")
     assert e.value.status == -5  # SP_ERR_CUDA
+    with pytest.raises(slide.SlideError) as e:
+        slide.probe_int_issue(1 << 10, 1)
+    assert e.value.status == -5
