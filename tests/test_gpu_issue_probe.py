@@ -11,10 +11,13 @@ def test_int_issue_rate_is_plausible_and_scales():
     import torch
     import slide
     torch.cuda.set_device(0)
+    slide.probe_int_issue(1 << 16, 1)  # lets the SM clock settle
     before = slide.kernel_launch_count()
     r1, ms1 = slide.probe_int_issue(1 << 15, 3)
     r2, ms2 = slide.probe_int_issue(1 << 16, 3)
     assert slide.kernel_launch_count() - before == 8
     for r in (r1, r2):
         assert 5e12 < r < 1e14, r
-    assert 1.6 < ms2 / ms1 < 2.4, (ms1, ms2)
+    # twice the steps take about twice as long (a loop the compiler had
+    # removed would give about 1)
+    assert 1.4 < ms2 / ms1 < 2.8, (ms1, ms2)
