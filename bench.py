@@ -147,7 +147,7 @@ def cpu_sample(w, states, budget_s, threads):
 
 
 def run_reference(args):
-    world, rank, _ = dist_setup()
+    _, rank, _ = dist_setup()
     if rank != 0:
         return
     w, states = workload(0)

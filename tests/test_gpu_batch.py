@@ -24,5 +24,5 @@ def test_batch_4096_mixed(gpu_solver, pdb15_tables):
         assert 0.0 < r["seconds"] <= st["wall_ms"] / 1000.0 + 1e-6, i
     pick = np.random.default_rng(4096).choice(4096, 32, replace=False)
     want = oracle.solve(w, states[pick], oracle.PDB, pdb15_tables)
-    for j, (i, b) in enumerate(zip(pick, want)):
+    for i, b in zip(pick, want):
         assert_same(got[i], b, states[i], w, "batch/%d" % i)
