@@ -48,3 +48,35 @@ def test_replay_helper():
     one = g.copy()
     one[0], one[1] = 1, 0
     assert slide.is_solution(one, bytes([2]), 4)
+
+
+def test_benchmark_configurations():
+    """The seeded workloads of the benchmark plan: sizes, widths, solvable
+    permutations, reproducible, and the bench headline's batch is the
+    `15_random` configuration."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    want = {"15_md_walk60": (4, 100), "15_random": (4, 100), "15_mixed4096": (4, 4096),
+            "24_walk120": (5, 50), "24_walk160": (5, 50), "24_walk200": (5, 50)}
+    for name, (w, n) in want.items():
+        gw, a = instances.config_instances(name)
+        assert (gw, a.shape, a.dtype) == (w, (n, w * w), np.uint8), name
+        gw2, b = instances.config_instances(name)
+        assert np.array_equal(a, b), name
+        assert all(instances.is_solvable(s, w) for s in a), name
+        assert all(sorted(s.tolist()) == list(range(w * w)) for s in a), name
+    # walks stay within their length in Manhattan distance
+    _, md60 = instances.config_instances("15_md_walk60")
+    assert max(instances.manhattan(s, 4) for s in md60) <= 60
+    _, mixed = instances.config_instances("15_mixed4096")
+    assert max(instances.manhattan(s, 4) for s in mixed[:2048]) <= 80
+    w, head = bench.workload(0)
+    assert w == 4 and np.array_equal(head, instances.config_instances("15_random")[1])
+    try:
+        instances.config_instances("nope")
+    except KeyError:
+        pass
+    else:
+        raise AssertionError("unknown configuration accepted")
