@@ -187,18 +187,22 @@ int sp_dfs_round(sp_solver *s, const uint8_t *roots, const int32_t *depth,
 
 /* sp_dfs_round for the Manhattan heuristic without allocating any memory.
  * No counterpart in the reference: it exists for callers that cannot call
- * cudaMalloc (code inside a stream capture that must stay free of allocation
- * nodes, hosts whose framework owns the device allocator, real-time loops
- * that must not enter the driver's allocator).  All pointers are device
- * pointers owned by the caller: d_roots n*width*width tiles, d_depth[n],
- * d_pre[n] as in sp_dfs_round, d_nodes[n] and d_found[1] receive its
- * outputs; stream is a cudaStream_t (NULL = default stream) and the call
- * returns after the stream has drained.  Scratch lives in a fixed device
- * array of about 7 MB that every GPU loading the library keeps until exit;
- * n above 16384 roots returns SP_ERR_CAPACITY.  Calls share that array:
- * calls overlapping on the GPU race, so serialise them.  The first call on a
- * device sets the array up (cudaGetSymbolAddress, table copy): make it before
- * any stream capture begins. */
+ * cudaMalloc -- hosts whose framework owns the device allocator (a caching
+ * pool that must account for every device byte, or a memory budget fixed at
+ * start-up) and real-time loops that must not enter the driver's allocator,
+ * whose latency is unbounded.  All pointers are device pointers owned by the
+ * caller: d_roots n*width*width tiles, d_depth[n], d_pre[n] as in
+ * sp_dfs_round, d_nodes[n] and d_found[1] receive its outputs; stream is a
+ * cudaStream_t (NULL = default stream).  The call is synchronous: it copies
+ * the device status back and returns after the stream has drained.  Scratch
+ * lives in a fixed device array of about 7 MB that every GPU loading the
+ * library keeps until exit; n above 16384 roots returns SP_ERR_CAPACITY
+ * before anything is launched.  Calls share that array and each re-writes
+ * what must start clean: calls overlapping on the GPU race, so serialise
+ * them.  Every call takes the array's device address on the current device
+ * (cudaGetSymbolAddress) and rebuilds its tables there.  A CUDA error the
+ * caller left pending is returned as SP_ERR_CUDA without being cleared;
+ * after any error return d_nodes and d_found are undefined. */
 int sp_dfs_round_md_noalloc(int width, const uint8_t *d_roots, const int32_t *d_depth,
                             const int32_t *d_pre, int n, int limit, uint64_t *d_nodes,
                             int32_t *d_found, void *stream);
@@ -243,6 +247,19 @@ int sp_selftest_stall(sp_solver *s, int timeout_ms, int32_t *device_status);
  * (1..2^24) steps; the best of `reps` (1..100) timed launches is reported,
  * its duration in *best_ms (may be NULL).  SP_ERR_CUDA without a GPU. */
 int sp_probe_int_issue(int32_t iters, int32_t reps, double *lane_ops_per_s, double *best_ms);
+
+/* Measured rate of random one-byte reads from a device buffer of
+ * working_set_bytes (4096 .. 2^32-1), one byte per lane at independent
+ * addresses through the read-only path, as the pattern-database search reads
+ * its tables (no counterpart in the reference): the roofline denominator of
+ * the PDB search, which each read costs one 32-byte sector.  A working set
+ * inside the 129 MB L2 (the 15-puzzle's 3 MB of tables) measures L2; one
+ * beyond it (the 24-puzzle's 488 MB) mostly DRAM.  One wave of resident
+ * blocks runs `iters` (1..2^20) rounds of 8 reads per thread; the best of
+ * `reps` (1..100) timed launches is reported, its duration in *best_ms (may
+ * be NULL).  Allocates and frees its buffer.  SP_ERR_CUDA without a GPU. */
+int sp_probe_random_sectors(uint64_t working_set_bytes, int32_t iters, int32_t reps, double *reads_per_s,
+                            double *best_ms);
 
 int sp_last_stats(const sp_solver *s, sp_stats *out);
 const char *sp_status_string(int status);

@@ -411,3 +411,273 @@ int orc_solve_batch(const orc_heur *h, const uint8_t *tiles, int n, int mode,
   free(c);
   return ORC_OK;
 }
+
+/* ------------------------------------------------------------------ */
+/* all host threads on one instance (CPU baseline of the benchmark)     */
+/* ------------------------------------------------------------------ */
+
+/* The same search with every host thread working on one instance at a time:
+ * per threshold iteration the root is expanded breadth-first to a uniform
+ * depth (no duplicate detection, children counted and goal-tested exactly as
+ * dfs() counts and tests them), and the depth-first searches below the
+ * frontier nodes that pass the f-test are shared out to the threads.  Every
+ * node is generated by the same parent as in the serial search, so the
+ * per-iteration counts and the optimal length are the serial ones; the
+ * recorded path is that of the shortest goal in the first frontier subtree
+ * holding one.  The reference's CPU solvers are serial; this only lets the
+ * baseline use all host cores on batches whose hardest instance dominates. */
+
+#define SPLIT_MAX_DEPTH 20
+
+typedef struct {
+  uint8_t board[25];
+  uint8_t inv[25];
+  uint8_t blank;
+  int8_t pre;
+  int h;
+  uint8_t path[SPLIT_MAX_DEPTH];
+} split_leaf;
+
+typedef struct {
+  uint64_t nodes;
+  int ans;
+  int ans_leaf;
+  uint8_t path[ORC_MAX_MOVES];
+} split_tres;
+
+typedef struct {
+  const hctx *c;
+  int threads;
+  pthread_barrier_t start, end;
+  int quit;
+  /* the current iteration's frontier */
+  const split_leaf *leaves;
+  int n_leaves, depth, limit;
+  int next;
+  split_tres *tres;
+} split_job;
+
+static void split_run(split_job *job, int tid, searcher *s) {
+  split_tres *r = &job->tres[tid];
+  r->nodes = 0;
+  r->ans = -1;
+  r->ans_leaf = -1;
+  for (;;) {
+    int i = __atomic_fetch_add(&job->next, 1, __ATOMIC_RELAXED);
+    if (i >= job->n_leaves) break;
+    const split_leaf *L = &job->leaves[i];
+    memcpy(s->board, L->board, sizeof s->board);
+    memcpy(s->inv, L->inv, sizeof s->inv);
+    s->blank = L->blank;
+    s->h = L->h;
+    s->limit = job->limit;
+    s->ans = -1;
+    s->have_path = 0;
+    s->nodes = 0;
+    memcpy(s->path, L->path, (size_t)job->depth);
+    dfs(s, job->depth, L->pre);
+    r->nodes += s->nodes;
+    if (s->ans >= 0 && (r->ans < 0 || s->ans < r->ans || (s->ans == r->ans && i < r->ans_leaf))) {
+      r->ans = s->ans;
+      r->ans_leaf = i;
+      memcpy(r->path, s->best_path, (size_t)(s->ans <= ORC_MAX_MOVES ? s->ans : ORC_MAX_MOVES));
+    }
+  }
+}
+
+typedef struct {
+  split_job *job;
+  int tid;
+} split_arg;
+
+static void *split_worker(void *arg) {
+  split_arg *a = (split_arg *)arg;
+  searcher *s = (searcher *)calloc(1, sizeof(searcher));
+  s->c = a->job->c;
+  s->mode = ORC_MODE_ALL;
+  for (;;) {
+    pthread_barrier_wait(&a->job->start);
+    if (a->job->quit) break;
+    split_run(a->job, a->tid, s);
+    pthread_barrier_wait(&a->job->end);
+  }
+  free(s);
+  return NULL;
+}
+
+/* One instance, all threads.  node_budget (0 = none) is checked between
+ * iterations. */
+static int split_solve(split_job *job, searcher *s0, const uint8_t *tiles, uint64_t budget, orc_result *out) {
+  const hctx *c = job->c;
+  memset(out, 0, sizeof(*out));
+  out->len = -1;
+  double t0 = now_s();
+  int st = check_instance(c->w, tiles);
+  if (st != ORC_OK) { out->status = st; return st; }
+  split_leaf root;
+  memset(&root, 0, sizeof root);
+  for (int i = 0; i < c->n; ++i) {
+    root.board[i] = tiles[i];
+    root.inv[tiles[i]] = (uint8_t)i;
+    if (!tiles[i]) root.blank = (uint8_t)i;
+  }
+  root.pre = -1;
+  root.h = c->heuristic == ORC_HEUR_MD ? md_value(c, root.board) : pdb_value(c, root.inv);
+  const int target = 32 * job->threads;
+  split_leaf *cur = NULL, *nxt = NULL;
+  size_t cap_cur = 0, cap_nxt = 0;
+  uint64_t before = 0;
+  st = ORC_ERR_LIMIT;
+  for (int it = 0; it < ORC_MAX_ITERS; ++it) {
+    const int limit = root.h + 2 * it;
+    if (budget && before > budget) { st = ORC_ERR_NODE_BUDGET; break; }
+    /* breadth-first frontier */
+    uint64_t interior = 0;
+    int ans = -1;
+    uint8_t ans_path[SPLIT_MAX_DEPTH + 1];
+    size_t n_cur = 1;
+    if (cap_cur < 1) { cap_cur = 1024; cur = (split_leaf *)realloc(cur, cap_cur * sizeof(split_leaf)); }
+    cur[0] = root;
+    if (root.h == 0) ans = 0;
+    int depth = 0;
+    while (n_cur > 0 && n_cur < (size_t)target && depth < SPLIT_MAX_DEPTH) {
+      size_t n_nxt = 0;
+      for (size_t q = 0; q < n_cur; ++q) {
+        const split_leaf *P = &cur[q];
+        for (int d = 0; d < 4; ++d) {
+          int to;
+          if (!legal_move(c->w, P->blank, d, &to)) continue;
+          if (P->pre >= 0 && d == 3 - P->pre) continue;
+          ++interior;
+          split_leaf C = *P;
+          const int tile = C.board[to], from = C.blank;
+          C.board[from] = (uint8_t)tile;
+          C.board[to] = 0;
+          C.inv[tile] = (uint8_t)from;
+          C.inv[0] = (uint8_t)to;
+          C.blank = (uint8_t)to;
+          C.pre = (int8_t)d;
+          C.h = c->heuristic == ORC_HEUR_MD ? P->h - c->md[to][tile] + c->md[from][tile] : pdb_value(c, C.inv);
+          C.path[depth] = (uint8_t)d;
+          if (C.h == 0 && (ans < 0 || depth + 1 < ans)) {
+            ans = depth + 1;
+            memcpy(ans_path, C.path, (size_t)(depth + 1));
+          }
+          if (depth + 1 + C.h > limit) continue;  /* generated, not expanded */
+          if (n_nxt == cap_nxt) {
+            cap_nxt = cap_nxt ? 2 * cap_nxt : 1024;
+            nxt = (split_leaf *)realloc(nxt, cap_nxt * sizeof(split_leaf));
+          }
+          nxt[n_nxt++] = C;
+        }
+      }
+      split_leaf *tp = cur; cur = nxt; nxt = tp;
+      size_t tc = cap_cur; cap_cur = cap_nxt; cap_nxt = tc;
+      n_cur = n_nxt;
+      ++depth;
+    }
+    /* depth-first below the frontier, on every thread */
+    job->leaves = cur;
+    job->n_leaves = (int)n_cur;
+    job->depth = depth;
+    job->limit = limit;
+    job->next = 0;
+    uint64_t nodes = interior;
+    int leaf_ans = -1, leaf_at = -1, leaf_t = -1;
+    if (n_cur > 0 && depth > 0) {
+      pthread_barrier_wait(&job->start);
+      split_run(job, 0, s0);
+      pthread_barrier_wait(&job->end);
+      for (int t = 0; t < job->threads; ++t) {
+        const split_tres *r = &job->tres[t];
+        nodes += r->nodes;
+        if (r->ans >= 0 && (leaf_ans < 0 || r->ans < leaf_ans || (r->ans == leaf_ans && r->ans_leaf < leaf_at))) {
+          leaf_ans = r->ans;
+          leaf_at = r->ans_leaf;
+          leaf_t = t;
+        }
+      }
+    } else if (n_cur > 0) {
+      /* the root alone passed the f-test and the frontier never grew: search it here */
+      s0->limit = limit;
+      memcpy(s0->board, root.board, sizeof s0->board);
+      memcpy(s0->inv, root.inv, sizeof s0->inv);
+      s0->blank = root.blank;
+      s0->h = root.h;
+      s0->ans = -1;
+      s0->have_path = 0;
+      s0->nodes = 0;
+      dfs(s0, 0, -1);
+      nodes = s0->nodes;
+      if (s0->ans >= 0) {
+        leaf_ans = s0->ans;
+        leaf_t = -2;
+      }
+    }
+    out->f_limit[it] = limit;
+    out->nodes[it] = nodes;
+    out->n_iter = it + 1;
+    before += nodes;
+    if (leaf_ans >= 0 && (ans < 0 || leaf_ans < ans)) {
+      ans = leaf_ans;
+      const uint8_t *p = leaf_t >= 0 ? job->tres[leaf_t].path : s0->best_path;
+      out->n_moves = ans <= ORC_MAX_MOVES ? ans : 0;
+      memcpy(out->moves, p, (size_t)out->n_moves);
+    } else if (ans >= 0) {
+      out->n_moves = ans;
+      memcpy(out->moves, ans_path, (size_t)ans);
+    }
+    if (ans >= 0) {
+      out->len = ans;
+      st = ORC_OK;
+      break;
+    }
+  }
+  free(cur);
+  free(nxt);
+  out->nodes_total = before;
+  out->status = st;
+  out->seconds = now_s() - t0;
+  return st;
+}
+
+int orc_solve_batch_split(const orc_heur *h, const uint8_t *tiles, int n, uint64_t node_budget, int threads,
+                          orc_result *out) {
+  if (!h || !tiles || !out || n < 0 || (h->width != 4 && h->width != 5)) return ORC_ERR_ARG;
+  if (h->heuristic == ORC_HEUR_PDB)
+    for (int t = 0; t < orc_num_tables(h->width); ++t)
+      if (!h->tables[t]) return ORC_ERR_ARG;
+  if (n == 0) return ORC_OK;
+  if (threads < 1) threads = 1;
+  hctx *c = (hctx *)malloc(sizeof(hctx));
+  hctx_init(c, h);
+  split_job job;
+  memset(&job, 0, sizeof job);
+  job.c = c;
+  job.threads = threads;
+  job.tres = (split_tres *)calloc((size_t)threads, sizeof(split_tres));
+  pthread_barrier_init(&job.start, NULL, (unsigned)threads);
+  pthread_barrier_init(&job.end, NULL, (unsigned)threads);
+  pthread_t *tid = (pthread_t *)malloc(sizeof(pthread_t) * (size_t)threads);
+  split_arg *args = (split_arg *)malloc(sizeof(split_arg) * (size_t)threads);
+  for (int t = 1; t < threads; ++t) {
+    args[t].job = &job;
+    args[t].tid = t;
+    pthread_create(&tid[t], NULL, split_worker, &args[t]);
+  }
+  searcher *s0 = (searcher *)calloc(1, sizeof(searcher));
+  s0->c = c;
+  s0->mode = ORC_MODE_ALL;
+  for (int i = 0; i < n; ++i) split_solve(&job, s0, tiles + (size_t)i * (size_t)c->n, node_budget, &out[i]);
+  job.quit = 1;
+  pthread_barrier_wait(&job.start);
+  for (int t = 1; t < threads; ++t) pthread_join(tid[t], NULL);
+  pthread_barrier_destroy(&job.start);
+  pthread_barrier_destroy(&job.end);
+  free(s0);
+  free(args);
+  free(tid);
+  free(job.tres);
+  free(c);
+  return ORC_OK;
+}

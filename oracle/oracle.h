@@ -77,6 +77,15 @@ int orc_solve(const orc_heur *h, const uint8_t *tiles, int mode,
 int orc_solve_batch(const orc_heur *h, const uint8_t *tiles, int n, int mode,
                     uint64_t node_budget, int threads, orc_result *out);
 
+/* The same answers (status, length, per-iteration counts) with all `threads`
+ * working on one instance at a time: per iteration the root is expanded
+ * breadth-first to a uniform depth and the depth-first searches below that
+ * frontier are shared out.  Only ORC_MODE_ALL; node_budget (0 = none) is
+ * checked between iterations.  The CPU baseline's driver for batches whose
+ * hardest instance would otherwise run on one core. */
+int orc_solve_batch_split(const orc_heur *h, const uint8_t *tiles, int n, uint64_t node_budget,
+                          int threads, orc_result *out);
+
 /* Heuristic value of one state (for tests of the frontier / h kernels). */
 int orc_heuristic(const orc_heur *h, const uint8_t *tiles);
 

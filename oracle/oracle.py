@@ -47,6 +47,9 @@ def load():
         lib.orc_solve_batch.argtypes = [ctypes.POINTER(OrcHeur), ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                         ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(OrcResult)]
         lib.orc_solve_batch.restype = ctypes.c_int
+        lib.orc_solve_batch_split.argtypes = [ctypes.POINTER(OrcHeur), ctypes.c_void_p, ctypes.c_int,
+                                              ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(OrcResult)]
+        lib.orc_solve_batch_split.restype = ctypes.c_int
         lib.orc_heuristic.argtypes = [ctypes.POINTER(OrcHeur), ctypes.c_void_p]
         lib.orc_heuristic.restype = ctypes.c_int
         lib.orc_pdb_build.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
@@ -101,13 +104,21 @@ def _heur(width, heuristic, tabs):
     return h
 
 
-def solve(width, tiles, heuristic=MD, tabs=None, mode=ALL, threads=None, node_budget=0):
+def solve(width, tiles, heuristic=MD, tabs=None, mode=ALL, threads=None, node_budget=0, split=False):
+    """Solve a batch.  One instance per thread at a time; with split=True all
+    threads work on one instance at a time (orc_solve_batch_split: same
+    lengths and counts, ALL mode only, budget checked between iterations)."""
     a = np.ascontiguousarray(np.asarray(tiles, dtype=np.uint8)).reshape(-1, width * width)
     n = a.shape[0]
     res = (OrcResult * max(1, n))()
     h = _heur(width, heuristic, tabs)
     threads = threads or os.cpu_count() or 1
-    st = load().orc_solve_batch(ctypes.byref(h), a.ctypes.data, n, mode, node_budget, threads, res)
+    if split:
+        if mode != ALL:
+            raise ValueError("split solves support the all-solutions mode only")
+        st = load().orc_solve_batch_split(ctypes.byref(h), a.ctypes.data, n, node_budget, threads, res)
+    else:
+        st = load().orc_solve_batch(ctypes.byref(h), a.ctypes.data, n, mode, node_budget, threads, res)
     if st != 0:
         raise RuntimeError("orc_solve_batch failed: %d" % st)
     out = []

@@ -1,27 +1,31 @@
 // sp_dfs_round_md_noalloc: one Manhattan-heuristic threshold round over a
 // caller's root set that allocates no memory.
 //
-// Some callers cannot call cudaMalloc: code running while a CUDA stream is
-// being captured into a graph that must not contain allocation nodes,
-// embedders whose process owns the device allocator (a framework pool that
-// forbids foreign allocations), and tight real-time loops that must not hit
-// the driver's allocator at all.  They pass device buffers for the inputs and
-// outputs; everything else the round needs lives in one file-scope device
-// array of fixed size, g_noalloc_scratch below.  Every GPU that loads the
-// library holds that array (kNoAllocScratchBytes, about 7 MB) until the
-// process exits.
+// Some callers cannot call cudaMalloc: embedders whose process owns the
+// device allocator (a framework's caching pool that must see every device
+// allocation, or a memory budget fixed at start-up), and tight real-time
+// loops that must not enter the driver's allocator, whose latency is
+// unbounded.  They pass device buffers for the inputs and outputs;
+// everything else the round needs lives in one file-scope device array of
+// fixed size, g_noalloc_scratch below.  Every GPU that loads the library
+// holds that array (kNoAllocScratchBytes, about 7 MB) until the process
+// exits.
 //
 // Limits and sharing: at most kNoAllocMaxRoots roots per call and a task
 // pool of kNoAllocPoolCap slots; larger inputs are rejected with
 // SP_ERR_CAPACITY before anything is launched.  All calls share the one
-// array: each call re-initialises what must start clean (pool control block,
-// ring sequence numbers, solution slot, output counters), and two calls whose
-// work overlaps on the GPU (different streams, or different host threads)
-// race on it -- serialise them.
+// array, which keeps what the last call left there: each call
+// re-initialises what must start clean (heuristic tables, pool control
+// block, ring sequence numbers, solution slot, output counters), and two
+// calls whose work overlaps on the GPU (different streams, or different host
+// threads) race on it -- serialise them.
 //
-// Set-up: the first call on a device takes the array's device address with
-// cudaGetSymbolAddress and copies the heuristic tables into it; make that
-// first call before starting any stream capture.
+// Set-up: every call takes the array's device address on the current device
+// with cudaGetSymbolAddress (the host-side name g_noalloc_scratch is not a
+// device address) and writes the heuristic tables with a kernel, so nothing
+// is cached that a device reset could make stale; the SM count is cached
+// once per device.  The call is synchronous: it reads the device status back
+// and returns after the stream has drained.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -55,26 +59,24 @@ constexpr size_t kNoAllocScratchBytes = align_up(kOffHt5 + sizeof(HeurTables));
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-struct DeviceSetup {
-  bool done = false;
-  unsigned char *base = nullptr;  // device address of g_noalloc_scratch
-  int num_sms = 0;
-};
-DeviceSetup g_setup[kMaxDevices];
+int g_num_sms[kMaxDevices];  // 0 until read for that device
 std::mutex g_setup_mu;
 
-void host_md_tables(int w, HeurTables *ht) {
-  memset(ht, 0, sizeof(*ht));
-  const int n = w * w;
-  for (int d = 0; d < 4; ++d)
-    for (int c = 0; c < n; ++c)
-      for (int t = 0; t < n; ++t) {
-        const int b = c - move_delta(w, d);
-        int v = 0;
-        if (t && b >= 0 && b < n)
-          v = (abs(b / w - t / w) + abs(b % w - t % w)) - (abs(c / w - t / w) + abs(c % w - t % w));
-        ht->mdd[(d * n + c) * n + t] = (int8_t)v;
-      }
+// The Manhattan delta table of width W (HeurTables::mdd: the change of h when
+// the tile at `cell` slides into the blank after the blank's move d), one
+// entry per thread; the rest of the record is unused by this path.
+template <int W>
+__global__ void noalloc_tables_kernel(unsigned char *base) {
+  constexpr int N = W * W;
+  HeurTables *ht = (HeurTables *)(base + (W == 4 ? kOffHt4 : kOffHt5));
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 4 * N * N) return;
+  const int t = i % N, c = (i / N) % N, d = i / (N * N);
+  const int b = c - move_delta(W, d);
+  int v = 0;
+  if (t && b >= 0 && b < N)
+    v = (abs(b / W - t / W) + abs(b % W - t % W)) - (abs(c / W - t / W) + abs(c % W - t % W));
+  ht->mdd[i] = (int8_t)v;
 }
 
 // Root records from the caller's device arrays; Manhattan distance of each
@@ -164,22 +166,21 @@ __global__ void noalloc_found_init_kernel(int32_t *found, unsigned char *base) {
   ((PoolCtl *)(base + kOffCtl))->error = 0;
 }
 
-int setup_device(int dev) {
-  std::lock_guard<std::mutex> lock(g_setup_mu);
-  DeviceSetup &d = g_setup[dev];
-  if (d.done) return SP_OK;
+// The scratch array's device address on the current device `dev` and that
+// device's SM count.  The address is taken on every call (it is cheap) so
+// that a new primary context after a device reset is picked up.
+int setup_device(int dev, unsigned char **base, int *num_sms) {
   void *ptr = nullptr;
   if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return SP_ERR_CUDA;
-  if (cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return SP_ERR_CUDA;
-  HeurTables h4, h5;
-  host_md_tables(4, &h4);
-  host_md_tables(5, &h5);
-  unsigned char *base = (unsigned char *)ptr;
-  if (cudaMemcpy(base + kOffHt4, &h4, sizeof(HeurTables), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(base + kOffHt5, &h5, sizeof(HeurTables), cudaMemcpyHostToDevice) != cudaSuccess)
+  *base = (unsigned char *)ptr;
+  std::lock_guard<std::mutex> lock(g_setup_mu);
+  if (!g_num_sms[dev] &&
+      (cudaDeviceGetAttribute(&g_num_sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+       g_num_sms[dev] < 1)) {
+    g_num_sms[dev] = 0;
     return SP_ERR_CUDA;
-  d.base = base;
-  d.done = true;
+  }
+  *num_sms = g_num_sms[dev];
   return SP_OK;
 }
 
@@ -194,15 +195,27 @@ extern "C" int sp_dfs_round_md_noalloc(int width, const uint8_t *d_roots, const 
   if ((width != 4 && width != 5) || n < 0 || (n > 0 && (!d_roots || !d_depth || !d_pre || !d_nodes)) || !d_found)
     return SP_ERR_ARG;
   if (n > kNoAllocMaxRoots) return SP_ERR_CAPACITY;
+  // an error the caller left pending is the caller's: report it without
+  // clearing it, and launch nothing
+  if (cudaPeekAtLastError() != cudaSuccess) return SP_ERR_CUDA;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return SP_ERR_CUDA;
-  const int rc = setup_device(dev);
+  unsigned char *base = nullptr;
+  int num_sms = 0;
+  const int rc = setup_device(dev, &base, &num_sms);
   if (rc) return rc;
-  const DeviceSetup &d = g_setup[dev];
   cudaStream_t st = (cudaStream_t)stream;
-  unsigned char *base = d.base;
+  // each launch is checked at once; after a failed one the outputs are undefined
+  auto launched = [](int k) {
+    note_launch(k);
+    return cudaGetLastError() == cudaSuccess;
+  };
+  const int nt = 4 * width * width * width * width;
+  if (width == 4) noalloc_tables_kernel<4><<<(nt + 255) / 256, 256, 0, st>>>(base);
+  else noalloc_tables_kernel<5><<<(nt + 255) / 256, 256, 0, st>>>(base);
+  if (!launched(1)) return SP_ERR_CUDA;
   noalloc_found_init_kernel<<<1, 1, 0, st>>>(d_found, base);
-  note_launch();
+  if (!launched(1)) return SP_ERR_CUDA;
   if (n > 0) {
     const int blocks = (n + 127) / 128;
     if (width == 4)
@@ -211,8 +224,9 @@ extern "C" int sp_dfs_round_md_noalloc(int width, const uint8_t *d_roots, const 
     else
       noalloc_prepare_kernel<5><<<blocks, 128, 0, st>>>(d_roots, d_depth, d_pre, n, limit, base, d_found,
                                                         (unsigned long long *)d_nodes);
+    if (!launched(1)) return SP_ERR_CUDA;
     noalloc_pool_kernel<<<(kNoAllocPoolCap + 255) / 256, 256, 0, st>>>(base, n);
-    note_launch(2);
+    if (!launched(1)) return SP_ERR_CUDA;
     RoundParams P{};
     P.subs = (const SubRoot *)(base + kOffSubs);
     P.tasks = (Task *)(base + kOffTasks);
@@ -229,15 +243,14 @@ extern "C" int sp_dfs_round_md_noalloc(int width, const uint8_t *d_roots, const 
     P.donate = 1;
     P.timeout_ns = 20000000000ull;
     P.poll_ns = 2000;
-    const uint32_t lanes = (uint32_t)d.num_sms * 1024u;
+    const uint32_t lanes = (uint32_t)num_sms * 1024u;
     P.reserve = lanes / 16u;
     P.spread = lanes / 32u;
     int grid = 0;
-    if (launch_search_round(width, false, 256, 0, d.num_sms, P, st, &grid) != cudaSuccess) return SP_ERR_CUDA;
+    if (launch_search_round(width, false, 256, 0, num_sms, P, st, &grid) != cudaSuccess) return SP_ERR_CUDA;
   }
   noalloc_finish_kernel<<<1, 1, 0, st>>>(base, d_found);
-  note_launch();
-  if (cudaGetLastError() != cudaSuccess) return SP_ERR_CUDA;
+  if (!launched(1)) return SP_ERR_CUDA;
   int32_t err = 0;
   if (cudaMemcpyAsync(&err, base + kOffCtl + offsetof(PoolCtl, error), sizeof(err), cudaMemcpyDeviceToHost, st) !=
           cudaSuccess ||

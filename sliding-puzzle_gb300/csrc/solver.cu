@@ -923,6 +923,8 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
       R->f_limit[I.iter] = L;
       R->nodes[I.iter] = interior_nodes(I, L);
       R->nodes_total += R->nodes[I.iter];
+      s->stats.nodes += R->nodes[I.iter];
+      s->stats.round_nodes[std::min(I.iter, SP_MAX_ROUNDS - 1)] += R->nodes[I.iter];
       R->n_iter = I.iter + 1;
       const int hg = tree_goal(I, L);
       if (hg >= 0) {

@@ -108,6 +108,8 @@ def load(build=True):
         "sp_gemm_bf16_nt": (I32, [P, P, P, I32, I32, I32]),
         "sp_selftest_stall": (I32, [P, I32, P]),
         "sp_probe_int_issue": (I32, [I32, I32, P, P]),
+        "sp_probe_random_sectors": (I32, [U64, I32, I32, P, P]),
+        "sp_dfs_round_md_noalloc": (I32, [I32, P, P, P, I32, I32, P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -416,6 +418,32 @@ def probe_int_issue(iters=1 << 16, reps=3):
     if st != 0:
         raise SlideError(st, "sp_probe_int_issue failed: %s" % lib.sp_status_string(st).decode())
     return rate.value, ms.value
+
+
+# Bytes a generated node of the PDB search reads, as the roofline charges
+# them: one regular and one reflected table entry, each its own 32-byte
+# sector (the pattern indices of different lanes never share a sector).
+PDB_BYTES_PER_NODE = 64
+SECTOR_BYTES = 32
+
+
+def probe_random_sectors(working_set_bytes, iters=256, reps=3):
+    """(random one-byte reads per second, best launch ms) from a device
+    buffer of `working_set_bytes`: the PDB search's roofline denominator
+    (sp_probe_random_sectors); x 32 bytes = sector bandwidth."""
+    lib = load()
+    rate, ms = ctypes.c_double(), ctypes.c_double()
+    st = lib.sp_probe_random_sectors(int(working_set_bytes), int(iters), int(reps), ctypes.byref(rate),
+                                     ctypes.byref(ms))
+    if st != 0:
+        raise SlideError(st, "sp_probe_random_sectors failed: %s" % lib.sp_status_string(st).decode())
+    return rate.value, ms.value
+
+
+def pdb_table_bytes(width):
+    """Bytes of the device lookup tables the PDB search reads (width 4: three
+    16^5-byte tables; width 5: two 25^6-byte tables)."""
+    return 3 * 16 ** 5 if width == 4 else 2 * 25 ** 6
 
 
 def replay(tiles, moves, width):

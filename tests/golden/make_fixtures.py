@@ -1,8 +1,9 @@
 """Regenerate the golden fixtures in this folder from the reference checkout.
 
-Run in a container where the reference is mounted (default /root/reference):
+Run in a container where the reference checkout is mounted:
 
-    python tests/golden/make_fixtures.py [REFERENCE_ROOT]
+    python tests/golden/make_fixtures.py REFERENCE_ROOT
+    SLIDE_REFERENCE_DIR=REFERENCE_ROOT python tests/golden/make_fixtures.py
 
 It copies, as JSON, the reference's own instance files and golden answers:
   korf100.json          benchmarks/korf100/probNNN + test/result_15puzzle.txt
@@ -83,4 +84,7 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SLIDE_REFERENCE_DIR")
+    if not ref:
+        sys.exit("usage: make_fixtures.py REFERENCE_ROOT (or set SLIDE_REFERENCE_DIR)")
+    main(ref)

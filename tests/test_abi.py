@@ -76,6 +76,14 @@ def test_rejects_bad_arguments_without_gpu():
     assert lib.sp_probe_int_issue(0, 3, ctypes.byref(rate), None) == -1
     assert lib.sp_probe_int_issue((1 << 24) + 1, 3, ctypes.byref(rate), None) == -1
     assert lib.sp_probe_int_issue(1 << 16, 0, ctypes.byref(rate), None) == -1
+    assert lib.sp_probe_random_sectors(3 << 20, 64, 3, None, None) == -1
+    assert lib.sp_probe_random_sectors(1024, 64, 3, ctypes.byref(rate), None) == -1
+    assert lib.sp_probe_random_sectors(1 << 32, 64, 3, ctypes.byref(rate), None) == -1
+    assert lib.sp_probe_random_sectors(3 << 20, 0, 3, ctypes.byref(rate), None) == -1
+    assert lib.sp_probe_random_sectors(3 << 20, 64, 101, ctypes.byref(rate), None) == -1
+    # the allocation-free round checks its arguments before touching the GPU
+    assert lib.sp_dfs_round_md_noalloc(6, None, None, None, 0, 10, None, None, None) == -1
+    assert lib.sp_dfs_round_md_noalloc(4, None, None, None, -1, 10, None, None, None) == -1
 
 
 def test_no_cpu_fallback_when_no_gpu():
@@ -88,4 +96,7 @@ def test_no_cpu_fallback_when_no_gpu():
     assert e.value.status == -5  # SP_ERR_CUDA
     with pytest.raises(slide.SlideError) as e:
         slide.probe_int_issue(1 << 10, 1)
+    assert e.value.status == -5
+    with pytest.raises(slide.SlideError) as e:
+        slide.probe_random_sectors(3 << 20, 4, 1)
     assert e.value.status == -5

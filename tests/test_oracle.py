@@ -144,3 +144,23 @@ def test_oracle_matches_reference_binaries(pdb24_tables):
     gotp = oracle.solve(5, states, oracle.PDB, pdb24_tables)
     refp = ref_run.run_pdb24_expand(states, pdb24_tables)
     assert [(r["len"], r["nodes_total"]) for r in gotp] == refp
+
+
+def test_split_driver_matches_serial_search(pdb15_tables):
+    """orc_solve_batch_split (every host thread on one instance, the CPU
+    baseline's driver) gives the serial search's lengths and per-iteration
+    counts, and valid paths, for both heuristics and both widths."""
+    import instances
+    import slide
+    cases = [(4, oracle.MD, instances.random_walks(4, 24, (40, 70), seed=3), None),
+             (4, oracle.PDB, instances.random_permutations(4, 6, seed=5), pdb15_tables),
+             (5, oracle.MD, instances.random_walks(5, 6, 40, seed=6), None),
+             (4, oracle.MD, np.arange(16, dtype=np.uint8)[None, :], None)]
+    for w, heur, states, tabs in cases:
+        a = oracle.solve(w, states, heur, tabs)
+        for threads in (1, 3, 8):
+            b = oracle.solve(w, states, heur, tabs, threads=threads, split=True)
+            for i, (x, y) in enumerate(zip(a, b)):
+                assert (y["status"], y["len"], y["f_limit"], y["nodes"]) == \
+                    (x["status"], x["len"], x["f_limit"], x["nodes"]), (w, heur, threads, i)
+                assert slide.is_solution(states[i], y["moves"], w), (w, heur, threads, i)
