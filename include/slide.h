@@ -240,6 +240,15 @@ int sp_gemm_bf16_nt(const uint16_t *a, const uint16_t *b, float *c, int m, int n
  * stays usable.  Returns SP_OK when the launch itself worked. */
 int sp_selftest_stall(sp_solver *s, int timeout_ms, int32_t *device_status);
 
+/* Self-test of the tensor-core GEMM's bounded waits (no counterpart in the
+ * reference): a 128 x 256 x 256 GEMM of the learned balancer whose K chunk
+ * `starve_chunk` (0..3) is never copied into shared memory, so the wait for
+ * it has nothing to wait for.  The kernel must give up after timeout_ms
+ * (10..2000), wait for the copies it did issue, free its tensor memory and
+ * report SP_ERR_TIMEOUT in *device_status without faulting; later GEMMs
+ * work.  Returns SP_OK when the launch itself worked. */
+int sp_selftest_gemm_stall(int32_t starve_chunk, int32_t timeout_ms, int32_t *device_status);
+
 /* Measured 32-bit integer operation rate of the current device (lane
  * operations per second; no counterpart in the reference): the roofline
  * denominator of the Manhattan search, which is bound by integer issue.  One

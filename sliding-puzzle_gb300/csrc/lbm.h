@@ -64,6 +64,12 @@ class Model {
   // the tcgen05 GEMM on its own, for tests.
   static int gemm_nt(const uint16_t *A, const uint16_t *B, float *C, int M, int N, int K, cudaStream_t st,
                      std::string &err);
+  // Self-test of the GEMM's bounded waits: a 128 x 256 x 256 GEMM whose K
+  // chunk `starve_chunk` (0..3) never gets its copies, so the wait for it
+  // runs out after timeout_ms; *device_status = SP_ERR_TIMEOUT when the
+  // kernel gave up, drained its copies, freed its tensor memory and returned.
+  static int gemm_stall_selftest(int starve_chunk, int timeout_ms, int *device_status, cudaStream_t st,
+                                 std::string &err);
 
   uint64_t launches() const { return launches_; }
 

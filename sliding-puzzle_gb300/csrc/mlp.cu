@@ -70,6 +70,8 @@ struct EpiArgs {
   __nv_bfloat16 *dH1T;            // backward output
   float *gw3, *gb2, *gb3, *gb1, *loss;
   int *err;
+  unsigned long long wait_ns;  // limit of every mbarrier wait (0: 2 s)
+  int starve_kc1;              // self-test only: K chunk starve_kc1 - 1 gets no copies (0: none)
 };
 
 // ---- PTX wrappers ---------------------------------------------------------
@@ -95,15 +97,15 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait: false after 2 s without the phase completing.
-__device__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+// Bounded wait: false after limit_ns without the phase completing.
+__device__ bool mbar_wait(uint32_t bar, uint32_t parity, unsigned long long limit_ns) {
   unsigned long long t0 = 0;
   for (uint32_t i = 0;; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((i & 255u) == 255u) {
       const unsigned long long now = gtimer();
       if (!t0) t0 = now;
-      else if (now - t0 > 2000000000ull) return false;
+      else if (now - t0 > limit_ns) return false;
     }
   }
 }
@@ -229,21 +231,26 @@ __global__ void __launch_bounds__(128, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_holder;
 
+  const unsigned long long limit = E.wait_ns ? E.wait_ns : 2000000000ull;
   if (threadIdx.x == 0) {
     int issued = 0, consumed = 0;
     bool ok = nk > 0;
+    // chunk kc's copies; the self-test's starved chunk gets none, so the
+    // wait for it runs out (its stage's barrier never completes a phase)
     auto issue = [&](int kc) {
       const int s = kc % STAGES;
-      mbar_expect_tx(full0 + 8 * s, A_STAGE + B_STAGE);
-      tma_load_2d(&ta, smem_u32(sA + s * A_STAGE), full0 + 8 * s, (kc0 + kc) * BK, m0);
-      tma_load_2d(&tb, smem_u32(sB + s * B_STAGE), full0 + 8 * s, (kc0 + kc) * BK, 0);
+      if (kc0 + kc + 1 != E.starve_kc1) {
+        mbar_expect_tx(full0 + 8 * s, A_STAGE + B_STAGE);
+        tma_load_2d(&ta, smem_u32(sA + s * A_STAGE), full0 + 8 * s, (kc0 + kc) * BK, m0);
+        tma_load_2d(&tb, smem_u32(sB + s * B_STAGE), full0 + 8 * s, (kc0 + kc) * BK, 0);
+      }
       ++issued;
     };
     for (int kc = 0; kc < min(nk, STAGES); ++kc) issue(kc);
     for (int kc = 0; kc < nk && ok; ++kc) {
       const int s = kc % STAGES;
       const uint32_t ph = (uint32_t)(kc / STAGES) & 1u;
-      if (!mbar_wait(full0 + 8 * s, ph)) {
+      if (!mbar_wait(full0 + 8 * s, ph, limit)) {
         ok = false;
         break;
       }
@@ -256,7 +263,7 @@ __global__ void __launch_bounds__(128, 1)
         umma_bf16(tmem, ad + (uint64_t)(kk * 2), bd + (uint64_t)(kk * 2), kIdesc, (kc | kk) ? 1u : 0u);
       umma_commit(done0 + 8 * s);
       if (kc + STAGES < nk) {
-        if (!mbar_wait(done0 + 8 * s, ph)) {
+        if (!mbar_wait(done0 + 8 * s, ph, limit)) {
           ok = false;
           break;
         }
@@ -265,14 +272,15 @@ __global__ void __launch_bounds__(128, 1)
     }
     if (!ok) {
       // drain: copies in flight land before the CTA leaves (bounded)
-      for (int kc = consumed; kc < issued; ++kc) mbar_wait(full0 + 8 * (kc % STAGES), (uint32_t)(kc / STAGES) & 1u);
+      for (int kc = consumed; kc < issued; ++kc)
+        if (kc0 + kc + 1 != E.starve_kc1) mbar_wait(full0 + 8 * (kc % STAGES), (uint32_t)(kc / STAGES) & 1u, limit);
       *s_fail = 1;
       if (E.err) atomicExch(E.err, 1);
     }
     umma_commit(accum);  // arrives once every MMA issued above has completed
   }
   __syncthreads();
-  const bool have = mbar_wait(accum, 0) && !*(volatile int *)s_fail;
+  const bool have = mbar_wait(accum, 0, limit) && !*(volatile int *)s_fail;
   if (!have && E.err) atomicExch(E.err, 1);
   tc_fence_after();
 
@@ -872,6 +880,58 @@ int Model::train_step(const uint8_t *tiles, const int32_t *slack, const float *t
   }
   if (loss) *loss = hl;
   return SP_OK;
+}
+
+int Model::gemm_stall_selftest(int starve_chunk, int timeout_ms, int *device_status, cudaStream_t st,
+                               std::string &err) {
+  constexpr int M = BM, K = 4 * BK;
+  if (starve_chunk < 0 || starve_chunk >= K / BK || timeout_ms < 10 || timeout_ms > 2000 || !device_status) {
+    err = "selftest needs starve_chunk in [0, 4) and timeout_ms in [10, 2000]";
+    return SP_ERR_ARG;
+  }
+  *device_status = SP_OK;
+  void *dA = nullptr, *dB = nullptr, *dC = nullptr;
+  int *derr = nullptr;
+  int rc = SP_OK;
+  do {
+    if (cudaMalloc(&dA, (size_t)M * K * 2) || cudaMalloc(&dB, (size_t)H * K * 2) ||
+        cudaMalloc(&dC, (size_t)M * H * 4) || cudaMalloc((void **)&derr, sizeof(int))) {
+      err = "cudaMalloc failed";
+      rc = SP_ERR_CUDA;
+      break;
+    }
+    if (cudaMemsetAsync(dA, 0, (size_t)M * K * 2, st) || cudaMemsetAsync(dB, 0, (size_t)H * K * 2, st) ||
+        cudaMemsetAsync(derr, 0, sizeof(int), st)) {
+      err = "memset failed";
+      rc = SP_ERR_CUDA;
+      break;
+    }
+    CUtensorMap ta, tb;
+    if ((rc = make_map(&ta, dA, M, K, BM, err)) || (rc = make_map(&tb, dB, H, K, H, err))) break;
+    EpiArgs E{};
+    E.C = (float *)dC;
+    E.m_valid = M;
+    E.err = derr;
+    E.wait_ns = (unsigned long long)timeout_ms * 1000000ull;
+    E.starve_kc1 = starve_chunk + 1;
+    if (launch_gemm<EPI_F32>(ta, tb, 1, K / BK, 1, E, st) != cudaSuccess) {
+      err = "GEMM launch failed";
+      rc = SP_ERR_CUDA;
+      break;
+    }
+    int herr = 0;
+    if (cudaMemcpyAsync(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost, st) || cudaStreamSynchronize(st)) {
+      err = std::string("GEMM self-test failed: ") + cudaGetErrorString(cudaGetLastError());
+      rc = SP_ERR_CUDA;
+      break;
+    }
+    *device_status = herr ? SP_ERR_TIMEOUT : SP_OK;
+  } while (0);
+  if (dA) cudaFree(dA);
+  if (dB) cudaFree(dB);
+  if (dC) cudaFree(dC);
+  if (derr) cudaFree(derr);
+  return rc;
 }
 
 int Model::gemm_nt(const uint16_t *A, const uint16_t *Bm, float *C, int M, int N, int K, cudaStream_t st,

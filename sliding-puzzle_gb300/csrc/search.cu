@@ -201,7 +201,24 @@ __device__ __noinline__ void warp_advance(const RoundParams &P, uint32_t i, uint
       }
       return;
     }
-    const double avg = (double)tot / (double)na;
+    // next-iteration load of root q: its load times its predicted growth
+    // (learned balancer; otherwise the load itself, the instance's growth
+    // being common to all its roots)
+    auto pred_load = [&](uint32_t q) -> double {
+      double lq = (double)__ldcg(ld + q);
+      if (P.sub_growth && lq > 0.0) {
+        const int j = min(kGrowthSlacks - 1, max(0, (L - 2 - P.sub_maxf[base + q]) >> 1));
+        lq *= exp2((double)P.sub_growth[(size_t)(base + q) * kGrowthSlacks + j] * (1.0 / 16.0));
+      }
+      return lq;
+    };
+    double ptot = (double)tot;
+    if (P.sub_growth) {
+      ptot = 0.0;
+      for (uint32_t q = lane; q < na; q += 32) ptot += pred_load(q);
+      for (int o = 16; o; o >>= 1) ptot += __shfl_xor_sync(FULL, ptot, o);
+    }
+    const double avg = ptot / (double)na;
     for (uint32_t q = lane; q < ns; q += 32) nx[q] = 0;
     // longest first: bucket = binary exponent of load / average (0 = no load)
     auto bucket = [&](double lq) -> int {
@@ -212,7 +229,7 @@ __device__ __noinline__ void warp_advance(const RoundParams &P, uint32_t i, uint
     };
     hist[lane] = 0;
     __syncwarp();
-    for (uint32_t q = lane; q < na; q += 32) atomicAdd(&hist[bucket((double)__ldcg(ld + q))], 1u);
+    for (uint32_t q = lane; q < na; q += 32) atomicAdd(&hist[bucket(pred_load(q))], 1u);
     __syncwarp();
     const uint32_t c = hist[lane];
     uint32_t suf = c;  // roots in buckets >= lane
@@ -233,7 +250,7 @@ __device__ __noinline__ void warp_advance(const RoundParams &P, uint32_t i, uint
     __syncwarp();
     const uint32_t mask = P.cap - 1u;
     for (uint32_t q = lane; q < na; q += 32) {
-      const double lq = (double)__ldcg(ld + q);
+      const double lq = pred_load(q);
       const uint32_t t = t0 + atomicAdd(&hist[bucket(lq)], 1u);
       int kk = 0;
       const double piece = avg * SP_MULTI_PIECE;

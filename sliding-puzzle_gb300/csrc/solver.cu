@@ -67,6 +67,12 @@
 
 namespace sp {
 
+// Learned balancer: slacks above this are predicted as this one (the model
+// is trained on slacks 0..7), and a root's predicted growth per threshold
+// step is capped at 2^kLbmMaxStep.
+constexpr int kLbmMaxSlack = 7;
+constexpr double kLbmMaxStep = 6.0;
+
 static std::atomic<uint64_t> g_launches{0};
 void note_launch(int n) { g_launches.fetch_add((uint64_t)n); }
 
@@ -150,12 +156,14 @@ struct MultiBufs {
   int32_t *iter = nullptr, *fin = nullptr, *status = nullptr, *goal = nullptr, *subf = nullptr, *ifv = nullptr;
   uint32_t *out = nullptr, *base = nullptr, *nsub = nullptr, *ioff = nullptr, *ilen = nullptr;
   unsigned long long *icum = nullptr, *iter_nodes = nullptr, *loads = nullptr, *fin_ns = nullptr, *t0_ns = nullptr;
+  uint8_t *growth = nullptr;  // learned balancer: [n_subs][kGrowthSlacks] growth codes
   size_t cap_iter = 0, cap_fin = 0, cap_status = 0, cap_goal = 0, cap_subf = 0, cap_ifv = 0, cap_out = 0,
          cap_base = 0, cap_nsub = 0, cap_ioff = 0, cap_ilen = 0, cap_icum = 0, cap_iter_nodes = 0, cap_loads = 0,
-         cap_fin_ns = 0, cap_t0_ns = 0;
+         cap_fin_ns = 0, cap_t0_ns = 0, cap_growth = 0;
+  bool use_growth = false;  // the current launch has growth codes
   void release() {
     void *ptrs[] = {iter, fin,  status, goal, subf,       ifv,   out,    base,
-                    nsub, ioff, ilen,   icum, iter_nodes, loads, fin_ns, t0_ns};
+                    nsub, ioff, ilen,   icum, iter_nodes, loads, fin_ns, t0_ns, growth};
     for (void *p : ptrs) cudaFree(p);
   }
 };
@@ -661,6 +669,7 @@ int launch_round(sp_solver *s, const RoundPlan &plan, size_t n_subs, size_t n_in
     P.n_subs = (uint32_t)n_subs;
     P.static_split = (s->cfg.lb_mode == SP_LB_STATIC_STEAL || s->cfg.lb_mode == SP_LB_LEARNED) ? 1 : 0;
     P.handback_nodes = (unsigned long long)s->cfg.handback_nodes;
+    P.sub_growth = m.use_growth ? m.growth : nullptr;
     SP_CUDA(s, launch_search_multi(s->w, s->heur == SP_HEUR_PDB, block, s->cfg.blocks_per_sm, s->num_sms, P,
                                    s->st, &grid));
   } else {
@@ -695,8 +704,9 @@ int launch_round(sp_solver *s, const RoundPlan &plan, size_t n_subs, size_t n_in
 // levels by the device pre-pass -- the reference splits a root into
 // ceil(load/avg) pieces (src/24puzzle_block_parallel_with_pdb.cu:839-897) --
 // and whole roots are published in decreasing predicted size.  With the
-// learned balancer, a root that has no measured load (not active in the
-// previous round) is predicted by the model instead of counting as 0.
+// learned balancer every root's prediction comes from the model: its
+// measured load times its own predicted growth, or the model's size estimate
+// for a root the previous round did not search.
 int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int32_t> &limits,
                RoundPlan &plan) {
   const bool learned = s->cfg.lb_mode == SP_LB_LEARNED;
@@ -736,29 +746,53 @@ int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int3
   });
   double total = 0;
   for (double t : inst_total) total += t;
-  if (learned) {
-    // roots without a measured load: the model's prediction at this threshold
-    std::vector<uint32_t> q_sub, q_pos;
+  if (learned && nc) {
+    // The model predicts every active root: y(s) = log2(1 + nodes) of its
+    // subtree at slack s = (limit - g - h) / 2 (clamped to the slacks it was
+    // trained on).  A root measured in the previous round is predicted as
+    // that load times its own growth 2^(y(s) - y(s - 1)) (in place of the
+    // instance's common growth); a root without a measured load as 2^y(s) - 1.
+    std::vector<uint32_t> q_sub;
     std::vector<int32_t> q_slack;
+    std::vector<int32_t> lo_at(nc, -1);  // index of y(s - 1), -1 if not needed
+    q_sub.reserve(2 * nc);
+    q_slack.reserve(2 * nc);
     for (size_t i = 0; i < ni; ++i) {
       const Instance &I = inst[i];
       for (size_t q = 0; q < off[i + 1] - off[i]; ++q) {
-        if (I.last_load[q]) continue;
         const TreeNode &t = I.tree[(size_t)I.leaves[q]];
+        const int sl = std::min(kLbmMaxSlack, std::max(0, (limits[i] - (int)t.g - t.h) / 2));
         q_sub.push_back(I.sub_base + (uint32_t)q);
-        q_pos.push_back((uint32_t)(off[i] + q));
-        q_slack.push_back(std::max(0, (limits[i] - (int)t.g - t.h) / 2));
+        q_slack.push_back(sl);
+        if (I.last_load[q]) {
+          lo_at[off[i] + q] = (int32_t)q_sub.size();
+          q_sub.push_back(I.sub_base + (uint32_t)q);
+          q_slack.push_back(std::max(0, sl - 1));
+        }
       }
     }
-    if (!q_sub.empty()) {
-      std::vector<float> y(q_sub.size());
-      int rc = s->lbm->predict_subs(s->d_subs, q_sub.data(), q_slack.data(), (int)q_sub.size(), y.data(), s->st,
-                                    s->err);
-      if (rc) return rc;
-      s->stats.kernel_launches += 2 * (int)((q_sub.size() + 65535) / 65536);
-      for (size_t k = 0; k < q_sub.size(); ++k) {
-        const double p = std::exp2(std::min(60.0, std::max(0.0, (double)y[k]))) - 1.0;
-        pred[q_pos[k]] = p;
+    std::vector<float> y(q_sub.size());
+    int rc = s->lbm->predict_subs(s->d_subs, q_sub.data(), q_slack.data(), (int)q_sub.size(), y.data(), s->st,
+                                  s->err);
+    if (rc) return rc;
+    s->stats.kernel_launches += 2 * (int)((q_sub.size() + 65535) / 65536);
+    total = 0;
+    size_t at = 0;
+    for (size_t i = 0; i < ni; ++i) {
+      const Instance &I = inst[i];
+      for (size_t q = 0; q < off[i + 1] - off[i]; ++q) {
+        const size_t j = off[i] + q;
+        const double yh = std::min(60.0, std::max(0.0, (double)y[at]));
+        double p;
+        if (lo_at[j] >= 0) {
+          const double step = std::min(kLbmMaxStep, std::max(0.0, yh - (double)y[(size_t)lo_at[j]]));
+          p = (double)I.last_load[q] * std::exp2(step);
+          at += 2;
+        } else {
+          p = std::exp2(yh) - 1.0;
+          at += 1;
+        }
+        pred[j] = p;
         total += p;
       }
     }
@@ -978,6 +1012,40 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
   SP_CUDA(s, cudaMemsetAsync(s->d_sol, 0, ni * sizeof(Solution), s->st));
   SP_CUDA(s, cudaMemsetAsync(m.fin_ns, 0, ni * sizeof(unsigned long long), s->st));
   SP_CUDA(s, cudaMemsetAsync(m.t0_ns, 0xFF, sizeof(unsigned long long), s->st));
+  // learned balancer: every root's predicted growth per threshold step at
+  // each slack, 2^(y(j+1) - y(j)) from the model's log2 sizes y, coded as
+  // 16 * log2 in a byte; the device multiplies each root's measured load by
+  // it to order and split the next iteration
+  m.use_growth = false;
+  if (s->cfg.lb_mode == SP_LB_LEARNED && n_subs) {
+    if (!s->lbm || !s->lbm->ready()) {
+      s->err = "SP_LB_LEARNED without a model (sp_lbm_init / sp_lbm_import)";
+      return SP_ERR_ARG;
+    }
+    const int G = kGrowthSlacks;
+    std::vector<uint32_t> gi(n_subs * G);
+    std::vector<int32_t> gs(n_subs * G);
+    for (size_t q = 0; q < n_subs; ++q)
+      for (int j = 0; j < G; ++j) {
+        gi[q * G + j] = (uint32_t)q;
+        gs[q * G + j] = std::min(j, kLbmMaxSlack);
+      }
+    std::vector<float> y(gi.size());
+    rc = s->lbm->predict_subs(s->d_subs, gi.data(), gs.data(), (int)gi.size(), y.data(), s->st, s->err);
+    if (rc) return rc;
+    s->stats.kernel_launches += 2 * (int)((gi.size() + 65535) / 65536);
+    std::vector<uint8_t> code(n_subs * G);
+    for (size_t q = 0; q < n_subs; ++q)
+      for (int j = 0; j < G; ++j) {
+        const int a = std::min(j, G - 2);
+        const double step = (double)y[q * G + a + 1] - (double)y[q * G + a];
+        code[q * G + j] = (uint8_t)std::lround(16.0 * std::min(kLbmMaxStep, std::max(0.0, step)));
+      }
+    if ((rc = ensure(s, &m.growth, &m.cap_growth, code.size()))) return rc;
+    SP_CUDA(s, up(m.growth, code));
+    s->stats.h2d_bytes += code.size();
+    m.use_growth = true;
+  }
   s->stats.h2d_bytes += ni * 40 + h_subf.size() * 4 + h_if.size() * 12;
   const double pre_s = ms_since(t_start) / 1000.0;  // host part before the launch
   for (auto &I : inst)
@@ -1721,6 +1789,15 @@ int sp_gemm_bf16_nt(const uint16_t *a, const uint16_t *b, float *c, int m, int n
   if (!a || !b || !c) return SP_ERR_ARG;
   std::string err;
   return lbm::Model::gemm_nt(a, b, c, m, n, k, nullptr, err);
+}
+
+int sp_selftest_gemm_stall(int32_t starve_chunk, int32_t timeout_ms, int32_t *device_status) {
+  if (!device_status) return SP_ERR_ARG;
+  std::string err;
+  int st = 0;
+  const int rc = lbm::Model::gemm_stall_selftest(starve_chunk, timeout_ms, &st, nullptr, err);
+  *device_status = st;
+  return rc;
 }
 
 int sp_last_stats(const sp_solver *s, sp_stats *out) {

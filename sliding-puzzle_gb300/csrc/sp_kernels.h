@@ -50,7 +50,12 @@ struct RoundParams {
   uint32_t n_subs;
   int32_t static_split;
   unsigned long long handback_nodes;  // 0: never hand an instance back to the host
+  // learned balancer (null otherwise): per root, kGrowthSlacks codes of its
+  // predicted growth from slack j to j + 1 (factor 2^(code / 16)), slack
+  // counted from the root's prefix-maximum f
+  const uint8_t *sub_growth;
 };
+constexpr int kGrowthSlacks = 8;
 
 // One threshold round: grid = num_sms * blocks_per_sm (0 = occupancy maximum).
 cudaError_t launch_search_round(int w, bool pdb, int block, int blocks_per_sm, int num_sms,

@@ -107,6 +107,7 @@ def load(build=True):
         "sp_lbm_gradients": (I32, [P, P, P, P, I32, P, P]),
         "sp_gemm_bf16_nt": (I32, [P, P, P, I32, I32, I32]),
         "sp_selftest_stall": (I32, [P, I32, P]),
+        "sp_selftest_gemm_stall": (I32, [I32, I32, P]),
         "sp_probe_int_issue": (I32, [I32, I32, P, P]),
         "sp_probe_random_sectors": (I32, [U64, I32, I32, P, P]),
         "sp_dfs_round_md_noalloc": (I32, [I32, P, P, P, I32, I32, P, P, P]),
@@ -321,7 +322,8 @@ AUTOTUNE_SPACE = (
     ("persistent", (1, 0)),
     ("handback_nodes", (600000, 0, 100000, 3000000)),
     ("donate_reserve", (0, -1, 30000)),
-    ("frontier_target", (2048, 1024, 4096)),
+    ("donate_min_slack", (6, 4, 8, 10)),
+    ("frontier_target", (2048, 1024, 4096, 8192, 16384)),
 )
 
 
@@ -381,6 +383,49 @@ def autotune(solver, tiles, space=AUTOTUNE_SPACE, reps=2, clock=None, log=None):
     return cur, history
 
 
+def autotune_cache_path():
+    """Where autotune_cached keeps its results: $SLIDE_AUTOTUNE_CACHE, else
+    ~/.cache/slide/autotune.json."""
+    return os.environ.get("SLIDE_AUTOTUNE_CACHE") or os.path.join(os.path.expanduser("~"), ".cache", "slide",
+                                                                    "autotune.json")
+
+
+def autotune_key(device, solver, tiles):
+    """Cache key: the GPU, the puzzle, the heuristic and the batch size
+    (rounded down to a power of two: the best root-set size and loop shape
+    depend on how many instances share the GPU)."""
+    n = max(1, _as_tiles(tiles, solver.width).shape[0])
+    return "%s|w%d|%s|n%d" % (device, solver.width, solver.heuristic, 1 << (n.bit_length() - 1))
+
+
+def autotune_cached(solver, tiles, device, path=None, **kw):
+    """autotune() with a per-(GPU, puzzle, heuristic, batch size) cache of the
+    winning settings in a JSON file: a hit applies the stored settings
+    without timing anything.  Returns (settings, hit)."""
+    import json
+    path = path or autotune_cache_path()
+    key = autotune_key(device, solver, tiles)
+    cache = {}
+    if os.path.exists(path):
+        try:
+            with open(path) as f:
+                cache = json.load(f)
+        except (OSError, ValueError):
+            cache = {}
+    if key in cache:
+        cfg = {k: int(v) for k, v in cache[key].items() if k in dict(SpConfig._fields_)}
+        solver.set_config(**cfg)
+        return cfg, True
+    best, _ = autotune(solver, tiles, **kw)
+    cache[key] = best
+    os.makedirs(os.path.dirname(path) or ".", exist_ok=True)
+    tmp = path + ".%d.tmp" % os.getpid()
+    with open(tmp, "w") as f:
+        json.dump(cache, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+    return best, False
+
+
 def gemm_bf16_nt(a_bits, b_bits):
     """C = A . B^T on the tensor cores; A [m][k], B [256][k] as bf16 bit patterns (uint16)."""
     lib = load()
@@ -393,6 +438,17 @@ def gemm_bf16_nt(a_bits, b_bits):
     if st != 0:
         raise SlideError(st, "sp_gemm_bf16_nt failed: %s" % lib.sp_status_string(st).decode())
     return c
+
+
+def selftest_gemm_stall(starve_chunk=1, timeout_ms=50):
+    """Device status of a tensor-core GEMM one of whose K chunks is never
+    copied in (SP_ERR_TIMEOUT = -8 when its bounded waits work)."""
+    lib = load()
+    st = ctypes.c_int32(0)
+    rc = lib.sp_selftest_gemm_stall(int(starve_chunk), int(timeout_ms), ctypes.byref(st))
+    if rc != 0:
+        raise SlideError(rc, "sp_selftest_gemm_stall failed: %s" % lib.sp_status_string(rc).decode())
+    return int(st.value)
 
 
 def kernel_launch_count():

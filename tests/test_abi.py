@@ -81,6 +81,9 @@ def test_rejects_bad_arguments_without_gpu():
     assert lib.sp_probe_random_sectors(1 << 32, 64, 3, ctypes.byref(rate), None) == -1
     assert lib.sp_probe_random_sectors(3 << 20, 0, 3, ctypes.byref(rate), None) == -1
     assert lib.sp_probe_random_sectors(3 << 20, 64, 101, ctypes.byref(rate), None) == -1
+    assert lib.sp_selftest_gemm_stall(4, 50, ctypes.byref(st)) == -1
+    assert lib.sp_selftest_gemm_stall(0, 5, ctypes.byref(st)) == -1
+    assert lib.sp_selftest_gemm_stall(0, 50, None) == -1
     # the allocation-free round checks its arguments before touching the GPU
     assert lib.sp_dfs_round_md_noalloc(6, None, None, None, 0, 10, None, None, None) == -1
     assert lib.sp_dfs_round_md_noalloc(4, None, None, None, -1, 10, None, None, None) == -1

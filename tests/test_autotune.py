@@ -16,6 +16,7 @@ class FakeSolver:
     """solve_raw 'takes' a time that is lowest at tpb 128, steps 16, persistent 1."""
 
     width = 4
+    heuristic = "manhattan"
 
     def __init__(self, change_results_at=None):
         self.config = slide.SpConfig()
@@ -64,3 +65,26 @@ def test_autotune_rejects_settings_that_change_results():
     tiles = np.tile(np.arange(16, dtype=np.uint8), (2, 1))
     with pytest.raises(RuntimeError):
         slide.autotune(s, tiles, reps=1, clock=s.clock)
+
+
+def test_autotune_cache_per_gpu_puzzle_heuristic(tmp_path):
+    """A cache miss tunes and stores; a hit on the same (GPU, puzzle,
+    heuristic, batch size) applies the stored settings without timing; a
+    different GPU or batch size misses."""
+    path = str(tmp_path / "tune.json")
+    s = FakeSolver()
+    s.heuristic = "pdb"
+    tiles = np.tile(np.arange(16, dtype=np.uint8), (3, 1))
+    best, hit = slide.autotune_cached(s, tiles, "GB300", path=path, reps=1, clock=s.clock)
+    assert not hit and best["threads_per_block"] == 128
+    calls = s.calls
+    s2 = FakeSolver()
+    s2.heuristic = "pdb"
+    best2, hit2 = slide.autotune_cached(s2, tiles, "GB300", path=path, reps=1, clock=s2.clock)
+    assert hit2 and s2.calls == 0 and best2 == best and s2.config.threads_per_block == 128
+    _, hit3 = slide.autotune_cached(FakeSolver(), tiles, "B200", path=path, reps=1)
+    assert not hit3
+    s4 = FakeSolver()
+    s4.heuristic = "pdb"
+    _, hit4 = slide.autotune_cached(s4, np.tile(tiles, (4, 1)), "GB300", path=path, reps=1, clock=s4.clock)
+    assert not hit4 and calls > 0

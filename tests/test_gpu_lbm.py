@@ -104,15 +104,20 @@ def test_training_reduces_loss(gpu_solver):
     assert last < 0.25 * first, (first, last)
 
 
-def test_learned_lb_keeps_counts(gpu_solver):
+@pytest.mark.parametrize("loop", ["hybrid", "round", "persistent"])
+def test_learned_lb_keeps_counts(gpu_solver, loop):
+    """The model drives every root's predicted load -- in the round loop's
+    plan and in the device loop's longest-first order and split -- and no
+    count may change, whatever the (here untrained) model predicts."""
     s = gpu_solver(4, "manhattan")
     s.lbm_init(seed=5)
     states = instances.random_walks(4, 24, (60, 90), seed=21)
     want = oracle.solve(4, states, oracle.MD)
-    s.set_config(lb_mode="learned", frontier_target=256)
+    extra = {"round": dict(persistent=0), "persistent": dict(persistent=1, handback_nodes=0)}.get(loop, {})
+    s.set_config(lb_mode="learned", frontier_target=256, **extra)
     got = s.solve(states)
     for i, (a, b) in enumerate(zip(got, want)):
-        assert_same(a, b, states[i], 4, "learned/%d" % i)
+        assert_same(a, b, states[i], 4, "learned/%s/%d" % (loop, i))
 
 
 def test_learned_lb_pdb24_golden(gpu_solver):
