@@ -220,6 +220,7 @@ def run_reference(args):
                        "warmup_sample": "first 8 instances"},
             "instances_per_s": len(states) * len(vals) / secs,
             "nodes_per_step": vals[-1]["nodes"],
+            "step_seconds": [round(x["seconds"], 3) for x in vals],
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": vals[-1]["sample"]},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -719,7 +720,7 @@ def main():
                        "parallelism": "replicas" if world > 1 else "1 GPU",
                        "l2": "512 MB buffer written between timed steps",
                        "pdb_build_ms": round(pdb_ms, 2)},
-            "instances_per_s": world * n / (total_ms / 1000.0),
+            "instances_per_s": world * n * args.steps / (total_ms / 1000.0),
             "nodes_per_step": all_nodes / args.steps,
             "rounds_per_step": rounds / args.steps,
             "tasks_donated_per_step": donated / args.steps,
@@ -727,7 +728,7 @@ def main():
             "lane_step_fraction": lane_steps / max(1, lane_slots),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
                     "d2h_bytes_per_step": d2h // args.steps, "ms_per_step": e2e_total / args.steps,
-                    "instances_per_s": world * n / (e2e_total / 1000.0)},
+                    "instances_per_s": world * n * args.steps / (e2e_total / 1000.0)},
             "gpu_launches": launches,
             "roofline": roofline,
             "peaks_measured": peaks,
