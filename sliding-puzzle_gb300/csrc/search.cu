@@ -79,9 +79,6 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
 __device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
-__device__ __forceinline__ void st_relaxed(uint32_t *p, uint32_t v) {
-  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 __device__ __forceinline__ unsigned long long globaltimer() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
@@ -230,20 +227,9 @@ __device__ __noinline__ void warp_advance(const RoundParams &P, uint32_t i, uint
       frexp(lq / avg, &e);
       return min(31, max(1, e + 15));
     };
-    // Each lane handles roots q = lane + 32 j in chunks of kChunk, so that
-    // the loads of a chunk are in flight together (this runs on the critical
-    // path of the instance's chain of iterations).
-    constexpr int kChunk = 8;
     hist[lane] = 0;
     __syncwarp();
-    for (uint32_t q0 = lane; q0 < na; q0 += 32 * kChunk) {
-      double v[kChunk];
-#pragma unroll
-      for (int j = 0; j < kChunk; ++j) v[j] = q0 + 32u * j < na ? pred_load(q0 + 32u * j) : -1.0;
-#pragma unroll
-      for (int j = 0; j < kChunk; ++j)
-        if (v[j] >= 0.0) atomicAdd(&hist[bucket(v[j])], 1u);
-    }
+    for (uint32_t q = lane; q < na; q += 32) atomicAdd(&hist[bucket(pred_load(q))], 1u);
     __syncwarp();
     const uint32_t c = hist[lane];
     uint32_t suf = c;  // roots in buckets >= lane
@@ -263,61 +249,34 @@ __device__ __noinline__ void warp_advance(const RoundParams &P, uint32_t i, uint
     t0 = __shfl_sync(FULL, t0, 0);
     __syncwarp();
     const uint32_t mask = P.cap - 1u;
-    const double piece = avg * SP_MULTI_PIECE;
-    for (uint32_t q0 = lane; q0 < na; q0 += 32 * kChunk) {
-      uint32_t tq[kChunk];
-      int kq[kChunk];
-      bool go[kChunk];
-#pragma unroll
-      for (int j = 0; j < kChunk; ++j) {
-        const uint32_t q = q0 + 32u * j;
-        go[j] = q < na;
-        tq[j] = 0;
-        kq[j] = 0;
-        if (!go[j]) continue;
-        const double lq = pred_load(q);
-        tq[j] = t0 + atomicAdd(&hist[bucket(lq)], 1u);
-        if (P.static_split && piece > 0 && lq > 2.0 * piece) {
-          // static split from the loads just measured: a root with x pieces'
-          // load goes out as a split task of about log(x)/log(2.4) levels (the
-          // reference cuts it into ceil(load/avg) pieces,
-          // src/24puzzle_block_parallel_with_pdb.cu:839-897)
-          int kk = (int)ceil(log(lq / piece) / log(2.4));
-          kq[j] = max(0, min(kk, min(10, L - (int)P.subs[base + q].g - 1)));
-        }
+    for (uint32_t q = lane; q < na; q += 32) {
+      const double lq = pred_load(q);
+      const uint32_t t = t0 + atomicAdd(&hist[bucket(lq)], 1u);
+      int kk = 0;
+      const double piece = avg * SP_MULTI_PIECE;
+      if (P.static_split && piece > 0 && lq > 2.0 * piece) {
+        // static split from the loads just measured: a root with x pieces'
+        // load goes out as a split task of about log(x)/log(2.4) levels (the
+        // reference cuts it into ceil(load/avg) pieces,
+        // src/24puzzle_block_parallel_with_pdb.cu:839-897)
+        kk = (int)ceil(log(lq / piece) / log(2.4));
+        kk = max(0, min(kk, min(10, L - (int)P.subs[base + q].g - 1)));
       }
-      // the ring slots are normally free at once (their previous occupants
-      // were claimed long before): relaxed reads of the whole chunk, a
-      // bounded wait only for a slot still occupied
-#pragma unroll
-      for (int j = 0; j < kChunk; ++j) {
-        if (!go[j] || ld_volatile(&P.seq[tq[j] & mask]) == tq[j]) continue;
-        bool free_slot = false;
-        for (int spin = 0; spin < (1 << 14) && !free_slot; ++spin) {
-          __nanosleep(64);
-          free_slot = ld_volatile(&P.seq[tq[j] & mask]) == tq[j];
-        }
-        if (!free_slot) {
-          if (atomicCAS(&ctl->error, 0, SP_ERR_CAPACITY) == 0) ctl->err_info[0] = tq[j];
-          go[j] = false;
-        }
+      bool free_slot = false;
+      for (int spin = 0; spin < (1 << 14) && !free_slot; ++spin) {
+        free_slot = ld_acquire(&P.seq[t & mask]) == t;
+        if (!free_slot) __nanosleep(64);
       }
-      // the claimants' copies out of these slots (seen through seq) happen
-      // before the new records are written; the records before their seq
-      __threadfence();
-#pragma unroll
-      for (int j = 0; j < kChunk; ++j) {
-        if (!go[j]) continue;
-        Task *D = &P.tasks[tq[j] & mask];
-        D->sub = base + q0 + 32u * j;
-        D->plen = 0;
-        D->mask = 0xF;
-        D->flags = (uint8_t)kq[j];
+      if (!free_slot) {
+        if (atomicCAS(&ctl->error, 0, SP_ERR_CAPACITY) == 0) ctl->err_info[0] = t;
+        continue;
       }
-      __threadfence();
-#pragma unroll
-      for (int j = 0; j < kChunk; ++j)
-        if (go[j]) st_relaxed(&P.seq[tq[j] & mask], tq[j] + 1u);
+      Task *D = &P.tasks[t & mask];
+      D->sub = base + q;
+      D->plen = 0;
+      D->mask = 0xF;
+      D->flags = (uint8_t)kk;
+      st_release(&P.seq[t & mask], t + 1u);
     }
     __syncwarp();
     return;
