@@ -227,6 +227,14 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_sector_probe(args):
+    """The roofline denominators alone: random one-byte reads over the
+    15-puzzle's and the 24-puzzle's table sizes, and the integer issue rate."""
+    import torch
+    torch.cuda.set_device(0)
+    print(json.dumps({"probe": "sectors", **measure_peaks()}), flush=True)
+
+
 def run_probe(args):
     """Steady-state kernel probes, one threshold round each.  balanced: one
     root replicated `--roots` times (identical subtrees: no load imbalance,
@@ -542,7 +550,7 @@ def run_workload(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--probe", choices=["balanced", "mixed"], default=None)
+    ap.add_argument("--probe", choices=["balanced", "mixed", "sectors"], default=None)
     ap.add_argument("--workload", choices=["15_md_walk60", "15_mixed4096", "24_bins", "yama24", "lb_ab"],
                     default=None)
     ap.add_argument("--tuples", type=int, default=1_000_000,
@@ -573,6 +581,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-secondary", action="store_true")
     args = ap.parse_args()
+    if args.probe == "sectors":
+        return run_sector_probe(args)
     if args.probe:
         return run_probe(args)
     if args.workload:
