@@ -656,6 +656,7 @@ def main():
             step_ms.append(e0.elapsed_time(e1))
             st = solver.stats()
             kern_ms.append(st["kernel_ms"])
+            round_ms = [round(x, 3) for x in st["round_kernel_ms"]]
             rounds += st["rounds"]
             donated += st["tasks_donated"]
             lane_steps += st["dev_lane_steps"]
@@ -735,6 +736,8 @@ def main():
             "rounds_per_step": rounds / args.steps,
             "tasks_donated_per_step": donated / args.steps,
             "kernel_ms_per_step": kms / args.steps,
+            "step_ms": [round(x, 3) for x in step_ms],
+            "last_step_round_kernel_ms": round_ms,
             "lane_step_fraction": lane_steps / max(1, lane_slots),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
                     "d2h_bytes_per_step": d2h // args.steps, "ms_per_step": e2e_total / args.steps,
