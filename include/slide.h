@@ -207,6 +207,29 @@ int sp_dfs_round_md_noalloc(int width, const uint8_t *d_roots, const int32_t *d_
                             const int32_t *d_pre, int n, int limit, uint64_t *d_nodes,
                             int32_t *d_found, void *stream);
 
+/* Horie's host-callable search, the reference's one C entry point
+ * (idas_parallel_main, src_horie/idas_parallel_host.h:33-34,
+ * src_horie/idas_parallel.cu:239-244), for the 15-puzzle: each of n roots
+ * (d_input, n*16 tiles, device memory) is searched on its own, depth-first
+ * to f_limit (0..251; a child is entered when its depth below the root + 1
+ * + h <= f_limit, the root counting as depth 0), moves tried up, right,
+ * left, down without undoing the last one, and stops at its first goal.
+ * Row i of d_plan (device memory, n*SP_PLAN_STRIDE bytes) receives
+ * [len, move_1 ... move_len] or [-1] when the root has no goal within the
+ * limit ([-2]: the root's search ran past 30 s, which only a table that lets
+ * h fall without bound can cause).  d_h_diff_table (16*16*4 signed bytes,
+ * [tile][its cell][blank's move], the reference's init_mdist layout) and
+ * d_movable_table (16*4 bytes, [cell][move]) are device tables as the
+ * reference takes them; NULL selects the Manhattan tables the reference
+ * builds (src_horie/idas_parallel_host.c:88-129).  The initial h is the
+ * Manhattan distance, as in the reference.  Launches on stream (a
+ * cudaStream_t, NULL = default) and returns without waiting, like the
+ * reference; allocates nothing.  Not part of the optimal-solve path: a
+ * first goal in depth-first order need not be the shortest. */
+#define SP_PLAN_STRIDE 252
+int sp_idas_parallel(const uint8_t *d_input, int n, int8_t *d_plan, int f_limit, const int8_t *d_h_diff_table,
+                     const uint8_t *d_movable_table, void *stream);
+
 /* Learned load balancer (no reference counterpart; the reference balances
  * only from the previous round's measured loads,
  * src/24puzzle_block_parallel_with_pdb.cu:839-897).  An MLP

@@ -681,3 +681,87 @@ int orc_solve_batch_split(const orc_heur *h, const uint8_t *tiles, int n, uint64
   free(c);
   return ORC_OK;
 }
+
+/* ------------------------------------------------------------------ */
+/* Horie's per-root first-goal search (the reference's host-callable     */
+/* entry point)                                                         */
+/* ------------------------------------------------------------------ */
+
+/* Restates the depth-first search of src_horie/idas_parallel.cu:172-197
+ * (idas_internal) for one 15-puzzle root, recursively: moves in the order
+ * up, right, left, down; the reverse of the last move skipped (none at the
+ * root); a child entered when depth + 1 + h(child) <= f_limit, h updated by
+ * the table hd[tile][tile's cell][blank's move] (undone by the reverse move's
+ * entry, as state_move(dir_reverse(dir)) does); moves allowed by mov[cell]
+ * [move]; the search returns at the first goal (h == 0, the root included).
+ * Default tables: src_horie/idas_parallel_host.c:88-129.  The path is never
+ * allowed past ORC_PLAN_STRIDE - 1 moves. */
+#define ORC_PLAN_STRIDE 252
+
+typedef struct {
+  uint8_t board[16];
+  int blank, h, limit;
+  int8_t hd[16 * 16 * 4];
+  uint8_t mov[16 * 4];
+  uint8_t path[ORC_PLAN_STRIDE];
+} fp_ctx;
+
+static const int fp_delta[4] = {-4, 1, -1, 4};
+
+static void fp_slide(fp_ctx *c, int d) {
+  int to = c->blank + fp_delta[d], t = c->board[to];
+  c->h += c->hd[(t * 16 + to) * 4 + d];
+  c->board[c->blank] = (uint8_t)t;
+  c->board[to] = 0;
+  c->blank = to;
+}
+
+static int fp_dfs(fp_ctx *c, int depth, int last) {
+  if (c->h == 0) return depth;
+  for (int d = 0; d < 4; ++d) {
+    if (depth > 0 && d == 3 - last) continue;
+    if (!c->mov[c->blank * 4 + d]) continue;
+    int to = c->blank + fp_delta[d];
+    int nh = c->h + c->hd[(c->board[to] * 16 + to) * 4 + d];
+    if (depth + 1 + nh > c->limit || depth + 1 >= ORC_PLAN_STRIDE) continue;
+    fp_slide(c, d);
+    c->path[depth] = (uint8_t)d;
+    int r = fp_dfs(c, depth + 1, d);
+    if (r >= 0) return r;
+    fp_slide(c, 3 - d);
+  }
+  return -1;
+}
+
+int orc_first_path(const uint8_t *tiles, int f_limit, const int8_t *h_diff, const uint8_t *movable,
+                   int8_t *row) {
+  if (!tiles || !row || f_limit < 0 || f_limit > ORC_PLAN_STRIDE - 1) return ORC_ERR_ARG;
+  fp_ctx *c = (fp_ctx *)calloc(1, sizeof(fp_ctx));
+  c->limit = f_limit;
+  for (int t = 0; t < 16; ++t)
+    for (int i = 0; i < 16; ++i)
+      for (int d = 0; d < 4; ++d) {
+        int gx = t % 4, gy = t / 4, x = i % 4, y = i / 4, v;
+        if (d == 0) v = gy > y ? -1 : 1;
+        else if (d == 1) v = gx < x ? -1 : 1;
+        else if (d == 2) v = gx > x ? -1 : 1;
+        else v = gy < y ? -1 : 1;
+        c->hd[(t * 16 + i) * 4 + d] = h_diff ? h_diff[(t * 16 + i) * 4 + d] : (int8_t)v;
+      }
+  for (int i = 0; i < 16; ++i)
+    for (int d = 0; d < 4; ++d) {
+      int x = i % 4, y = i / 4;
+      int ok = d == 0 ? y > 0 : d == 1 ? x < 3 : d == 2 ? x > 0 : y < 3;
+      c->mov[i * 4 + d] = movable ? (movable[i * 4 + d] != 0) : (uint8_t)ok;
+    }
+  for (int i = 0; i < 16; ++i) {
+    c->board[i] = tiles[i] & 15u;
+    if (!c->board[i]) c->blank = i;
+    else c->h += abs(i % 4 - c->board[i] % 4) + abs(i / 4 - c->board[i] / 4);
+  }
+  int len = fp_dfs(c, 0, -1);
+  row[0] = (int8_t)len;
+  for (int i = 0; i < len; ++i) row[1 + i] = (int8_t)c->path[i];
+  free(c);
+  return ORC_OK;
+}

@@ -86,6 +86,14 @@ int orc_solve_batch(const orc_heur *h, const uint8_t *tiles, int n, int mode,
 int orc_solve_batch_split(const orc_heur *h, const uint8_t *tiles, int n, uint64_t node_budget,
                           int threads, orc_result *out);
 
+/* Horie's per-root search (src_horie/idas_parallel.cu:172-236): the first
+ * goal path of one 15-puzzle root in depth-first order within f_limit
+ * (0..251), into row = [len, moves...] or [-1].  h_diff (16*16*4,
+ * [tile][cell][blank's move]) and movable (16*4) may be NULL for the
+ * reference's Manhattan tables (src_horie/idas_parallel_host.c:88-129). */
+int orc_first_path(const uint8_t *tiles, int f_limit, const int8_t *h_diff, const uint8_t *movable,
+                   int8_t *row);
+
 /* Heuristic value of one state (for tests of the frontier / h kernels). */
 int orc_heuristic(const orc_heur *h, const uint8_t *tiles);
 

@@ -50,6 +50,9 @@ def load():
         lib.orc_solve_batch_split.argtypes = [ctypes.POINTER(OrcHeur), ctypes.c_void_p, ctypes.c_int,
                                               ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(OrcResult)]
         lib.orc_solve_batch_split.restype = ctypes.c_int
+        lib.orc_first_path.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p]
+        lib.orc_first_path.restype = ctypes.c_int
         lib.orc_heuristic.argtypes = [ctypes.POINTER(OrcHeur), ctypes.c_void_p]
         lib.orc_heuristic.restype = ctypes.c_int
         lib.orc_pdb_build.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
@@ -135,3 +138,21 @@ def heuristic(width, tiles, heuristic=MD, tabs=None):
     a = np.ascontiguousarray(np.asarray(tiles, dtype=np.uint8)).reshape(-1, width * width)
     h = _heur(width, heuristic, tabs)
     return np.array([load().orc_heuristic(ctypes.byref(h), a[i].ctypes.data) for i in range(a.shape[0])])
+
+
+PLAN_STRIDE = 252
+
+
+def first_paths(tiles, f_limit, h_diff=None, movable=None):
+    """Horie's per-root search on the CPU: one plan row per 15-puzzle root,
+    [len, moves...] or [-1] (orc_first_path)."""
+    a = np.ascontiguousarray(np.asarray(tiles, dtype=np.uint8)).reshape(-1, 16)
+    out = np.zeros((a.shape[0], PLAN_STRIDE), dtype=np.int8)
+    hd = None if h_diff is None else np.ascontiguousarray(np.asarray(h_diff, dtype=np.int8).reshape(-1))
+    mv = None if movable is None else np.ascontiguousarray(np.asarray(movable, dtype=np.uint8).reshape(-1))
+    for i in range(a.shape[0]):
+        st = load().orc_first_path(a[i].ctypes.data, int(f_limit), None if hd is None else hd.ctypes.data,
+                                   None if mv is None else mv.ctypes.data, out[i].ctypes.data)
+        if st != 0:
+            raise RuntimeError("orc_first_path failed: %d" % st)
+    return out

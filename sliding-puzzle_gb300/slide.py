@@ -16,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libslide.so")
 
 SP_MAX_ITERS = 96
+SP_PLAN_STRIDE = 252
 SP_MAX_MOVES = 240
 HEUR = {"manhattan": 0, "md": 0, "pdb": 1}
 LB = {"steal": 0, "static": 1, "static_steal": 1, "none": 2, "learned": 3}
@@ -111,6 +112,7 @@ def load(build=True):
         "sp_probe_int_issue": (I32, [I32, I32, P, P]),
         "sp_probe_random_sectors": (I32, [U64, I32, I32, P, P]),
         "sp_dfs_round_md_noalloc": (I32, [I32, P, P, P, I32, I32, P, P, P]),
+        "sp_idas_parallel": (I32, [P, I32, P, I32, P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -438,6 +440,20 @@ def gemm_bf16_nt(a_bits, b_bits):
     if st != 0:
         raise SlideError(st, "sp_gemm_bf16_nt failed: %s" % lib.sp_status_string(st).decode())
     return c
+
+
+def idas_parallel(d_input, n, d_plan, f_limit, d_h_diff_table=None, d_movable_table=None, stream=None):
+    """Horie's idas_parallel_main on device pointers (sp_idas_parallel):
+    every root searched on its own to f_limit, its first goal path in
+    depth-first order into its SP_PLAN_STRIDE-byte plan row.  Asynchronous
+    on `stream` (an int handle or None)."""
+    lib = load()
+    st = lib.sp_idas_parallel(ctypes.c_void_p(d_input), int(n), ctypes.c_void_p(d_plan), int(f_limit),
+                              ctypes.c_void_p(d_h_diff_table) if d_h_diff_table else None,
+                              ctypes.c_void_p(d_movable_table) if d_movable_table else None,
+                              ctypes.c_void_p(stream) if stream else None)
+    if st != 0:
+        raise SlideError(st, "sp_idas_parallel failed: %s" % lib.sp_status_string(st).decode())
 
 
 def selftest_gemm_stall(starve_chunk=1, timeout_ms=50):

@@ -164,3 +164,28 @@ def test_split_driver_matches_serial_search(pdb15_tables):
                 assert (y["status"], y["len"], y["f_limit"], y["nodes"]) == \
                     (x["status"], x["len"], x["f_limit"], x["nodes"]), (w, heur, threads, i)
                 assert slide.is_solution(states[i], y["moves"], w), (w, heur, threads, i)
+
+
+def test_first_path_restatement_semantics():
+    """orc_first_path, the CPU statement of Horie's per-root search: a root
+    finds a goal exactly when f_limit reaches its optimal length (Manhattan
+    is admissible), the path replays to the goal within f_limit, and it is
+    the first in depth-first order -- here checked as: never shorter than
+    optimal, and equal to optimal when f_limit is the optimal length."""
+    import instances
+    import slide
+    states = instances.random_walks(4, 24, (8, 30), seed=3)
+    opt = [r["len"] for r in oracle.solve(4, states, oracle.MD)]
+    for f in (0, 9, 14, 20, 26):
+        rows = oracle.first_paths(states, f)
+        for i, r in enumerate(rows):
+            L = int(r[0])
+            if f < opt[i]:
+                assert L == -1, (f, i)
+                continue
+            assert opt[i] <= L <= f and (L - opt[i]) % 2 == 0, (f, i)
+            assert slide.is_solution(states[i], bytes(r[1:1 + L].astype(np.uint8)), 4), (f, i)
+    exact = oracle.first_paths(states[:1], opt[0])
+    assert int(exact[0][0]) == opt[0]
+    goal = oracle.first_paths(np.arange(16, dtype=np.uint8), 0)
+    assert int(goal[0][0]) == 0
