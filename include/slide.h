@@ -219,7 +219,8 @@ int sp_dfs_round_md_noalloc(int width, const uint8_t *d_roots, const int32_t *d_
  * limit ([-2]: the root's search ran past 30 s, which only a table that lets
  * h fall without bound can cause).  d_h_diff_table (16*16*4 signed bytes,
  * [tile][its cell][blank's move], the reference's init_mdist layout) and
- * d_movable_table (16*4 bytes, [cell][move]) are device tables as the
+ * d_movable_table (16*4 bytes, [cell][move]; a move off the board is never
+ * made, whatever the table says) are device tables as the
  * reference takes them; NULL selects the Manhattan tables the reference
  * builds (src_horie/idas_parallel_host.c:88-129).  The initial h is the
  * Manhattan distance, as in the reference.  Launches on stream (a

@@ -752,7 +752,7 @@ int orc_first_path(const uint8_t *tiles, int f_limit, const int8_t *h_diff, cons
     for (int d = 0; d < 4; ++d) {
       int x = i % 4, y = i / 4;
       int ok = d == 0 ? y > 0 : d == 1 ? x < 3 : d == 2 ? x > 0 : y < 3;
-      c->mov[i * 4 + d] = movable ? (movable[i * 4 + d] != 0) : (uint8_t)ok;
+      c->mov[i * 4 + d] = (uint8_t)(ok && (!movable || movable[i * 4 + d] != 0));
     }
   for (int i = 0; i < 16; ++i) {
     c->board[i] = tiles[i] & 15u;

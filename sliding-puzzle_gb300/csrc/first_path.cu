@@ -59,8 +59,10 @@ __global__ void __launch_bounds__(kFpBlock) first_path_kernel(const uint8_t *inp
       s_hdiff[i] = (int8_t)v;
     }
   }
+  // a caller's movable table is also held to the board's edges, so that no
+  // table can move the blank off the board
   for (int i = threadIdx.x; i < kN * 4; i += kFpBlock)
-    s_mov[i] = movable_in ? (movable_in[i] ? 1 : 0) : (uint8_t)((legal_moves(kW, i / 4) >> (i % 4)) & 1u);
+    s_mov[i] = (uint8_t)((legal_moves(kW, i / 4) >> (i % 4)) & 1u) & (movable_in ? (movable_in[i] ? 1 : 0) : 1);
   __syncthreads();
 
   const int id = blockIdx.x * kFpBlock + threadIdx.x;
