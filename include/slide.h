@@ -65,8 +65,9 @@ typedef enum {
                               previous round's loads
                               (src/24puzzle_block_parallel_with_pdb.cu:839-897) */
   SP_LB_NONE = 2,          /* root set only: no re-split, no donation */
-  SP_LB_LEARNED = 3        /* SP_LB_STATIC_STEAL, with roots that have no measured
-                              load predicted by the learned model (sp_lbm_*) */
+  SP_LB_LEARNED = 3        /* SP_LB_STATIC_STEAL, every root's next load predicted
+                              by the learned model (sp_lbm_*): its measured load x
+                              its own predicted growth, or the model's size estimate */
 } sp_lb_mode;
 
 typedef struct {
