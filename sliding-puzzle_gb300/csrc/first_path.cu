@@ -87,7 +87,9 @@ __global__ void __launch_bounds__(kFpBlock) first_path_kernel(const uint8_t *inp
     blank = to;
   };
   int depth = 0, dir = 0;
-  uint32_t top = 0;  // stack word holding level depth - 1 (lower words in shared memory)
+  // the stack word holding level depth - 1, the last move made (completed
+  // words below it sit in shared memory)
+  uint32_t top = 0;
   auto last = [&]() -> int { return (int)((top >> (2 * ((depth - 1) & 15))) & 3u); };
   // a root whose search outlives the time limit (only a caller table that
   // lets h fall without bound can make one run that long) gives up: -2
@@ -117,7 +119,7 @@ __global__ void __launch_bounds__(kFpBlock) first_path_kernel(const uint8_t *inp
       if (depth + 1 + nh <= f_limit && depth + 1 < SP_PLAN_STRIDE) {
         apply(dir);
         const int sh = 2 * (depth & 15);
-        top = (top & ~(3u << sh)) | ((uint32_t)dir << sh);
+        top = sh ? (top & ~(3u << sh)) | ((uint32_t)dir << sh) : (uint32_t)dir;  // sh 0: a new word
         if ((depth & 15) == 15) s_stack[depth >> 4][tid] = top;
         ++depth;
         dir = 0;
@@ -129,9 +131,9 @@ __global__ void __launch_bounds__(kFpBlock) first_path_kernel(const uint8_t *inp
         row[0] = -1;
         return;
       }
-      --depth;
-      if ((depth & 15) == 15) top = s_stack[depth >> 4][tid];
+      --depth;  // undo the move of level depth, held in top
       dir = (int)((top >> (2 * (depth & 15))) & 3u);
+      if ((depth & 15) == 0 && depth > 0) top = s_stack[(depth >> 4) - 1][tid];
       apply(3 - dir);
     }
   }
