@@ -113,6 +113,33 @@ struct Idx<5> {
 };
 
 __device__ __forceinline__ uint32_t byte_sum(uint32_t v) { return __dp4a(v, 0x01010101u, 0u); }
+
+// The step's move arithmetic without compares: the four blank
+// displacements as signed bytes of one immediate, and for the 24-puzzle the
+// 4-bit legal-move mask of every cell packed into two 64-bit immediates
+// (measured: -3 % step time on the 15-puzzle for the first, +5 % nodes/s on
+// the 24-puzzle for both; the packed masks cost the 15-puzzle kernel a
+// spill, so it keeps legal_moves).
+constexpr uint64_t legal_pack(int w, int first, int count) {
+  uint64_t v = 0;
+  for (int c = 0; c < count; ++c) {
+    const int cell = first + c, r = cell / w, cc = cell % w;
+    const uint64_t m = (r > 0 ? 1u : 0u) | (cc < w - 1 ? 2u : 0u) | (cc > 0 ? 4u : 0u) | (r < w - 1 ? 8u : 0u);
+    v |= m << (4 * c);
+  }
+  return v;
+}
+template <int W>
+__device__ __forceinline__ uint32_t step_legal(int blank) {
+  if (W == 4) return legal_moves(W, blank);
+  const uint64_t w = blank < 16 ? legal_pack(5, 0, 16) : legal_pack(5, 16, 9);
+  return (uint32_t)(w >> (4 * (blank & 15))) & 15u;
+}
+template <int W>
+__device__ __forceinline__ int step_delta(int d) {
+  constexpr uint32_t pack = W == 4 ? 0x04FF01FCu : 0x05FF01FBu;  // -W, +1, -1, +W
+  return (int)(pack << (24 - 8 * d)) >> 24;
+}
 __device__ __forceinline__ uint32_t set_byte(uint32_t v, int p, uint32_t x) {
   return (v & ~(0xFFu << (8 * p))) | (x << (8 * p));
 }
@@ -557,7 +584,7 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
   // walks stay converged); only the child's table lookups, the f-test and
   // the stack bookkeeping differ.  Returns true when the task is exhausted.
   auto step = [&]() -> bool {
-    uint32_t cand = legal_moves(W, blank) & (0xFu << it);
+    uint32_t cand = step_legal<W>(blank) & (0xFu << it);
     if (pre >= 0) cand &= ~(1u << (3 - pre));
     if (k == 0) cand &= mask0;
     const bool gen = cand != 0;
@@ -570,7 +597,7 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
       if ((k & 15) == 15) top = s_stack[k >> 4][tid];
       dm = 3 - (int)((top >> (2 * (k & 15))) & 3u);  // the reverse of the move into level k + 1
     }
-    const int from = blank + move_delta(W, dm);
+    const int from = blank + step_delta<W>(dm);
     const int t = tile_at(from);  // slides from `from` into the blank's cell
     int nh;
     uint32_t nhvr = hvr, nhvf = hvf;
@@ -621,7 +648,7 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
       top = (top & ~(3u << sh)) | ((uint32_t)dm << sh);
       if ((k & 15) == 15) s_stack[k >> 4][tid] = top;
       ++k;
-      if (k < 64) cut &= ~(1ull << k);
+      if (cut && k < 64) cut &= ~(1ull << k);  // cut is almost always 0
       pre = dm;
       it = 0;
       if (nh == 0) record_goal();
@@ -636,7 +663,7 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
     } else {
       --g;
       it = (3 - dm) + 1;  // the next sibling of the undone move
-      if (k < 64 && ((cut >> k) & 1ull)) it = 4;
+      if (cut && k < 64 && ((cut >> k) & 1ull)) it = 4;
       if (k == 0) pre = rpre;
       else if (k & 15) pre = (int)((top >> (2 * ((k - 1) & 15))) & 3u);
       else pre = (int)((s_stack[(k - 1) >> 4][tid] >> 30) & 3u);
