@@ -584,8 +584,9 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
   // walks stay converged); only the child's table lookups, the f-test and
   // the stack bookkeeping differ.  Returns true when the task is exhausted.
   auto step = [&]() -> bool {
-    uint32_t cand = step_legal<W>(blank) & (0xFu << it);
-    if (pre >= 0) cand &= ~(1u << (3 - pre));
+    // minus the reverse of the move into this node: its bit from a nibble
+    // table indexed by pre + 1 (pre = -1 at a task root without one)
+    uint32_t cand = step_legal<W>(blank) & (0xFu << it) & ~((0x12480u >> (4 * (pre + 1))) & 15u);
     if (k == 0) cand &= mask0;
     const bool gen = cand != 0;
     if (!gen && k == 0) return true;
