@@ -200,6 +200,9 @@ def run_reference(args):
     _, rank, _ = dist_setup()
     if rank != 0:
         return
+    # the table build's OpenMP threads must not spin on the cores the timed
+    # search runs on (set before the oracle library loads the runtime)
+    os.environ.setdefault("OMP_WAIT_POLICY", "PASSIVE")
     oracle = oracle_module()
     w, states = workload(0)
     tabs = oracle.tables(w)
