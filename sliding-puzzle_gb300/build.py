@@ -15,7 +15,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libslide.so")
 SOURCES = ["search.cu", "pdb_build.cu", "solver.cu", "noalloc.cu", "mlp.cu", "issue_probe.cu", "sector_probe.cu",
-           "first_path.cu"]
+           "first_path.cu", "frontier.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include")]

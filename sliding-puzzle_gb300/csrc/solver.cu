@@ -1,6 +1,7 @@
 // Host side of libslide: the C ABI (include/slide.h), the root-set
-// ("frontier") construction, the IDA* threshold-round loop and static load
-// balancing.  Device work is in search.cu, pdb_build.cu and mlp.cu.
+// ("frontier") templates, the IDA* threshold-round loop and static load
+// balancing.  Device work is in search.cu, frontier.cu (the root sets
+// themselves), pdb_build.cu and mlp.cu.
 //
 // A batch is solved in two phases by default: one persistent launch runs
 // every instance's small iterations on the device (solve_multi); an instance
@@ -78,15 +79,18 @@ void note_launch(int n) { g_launches.fetch_add((uint64_t)n); }
 
 namespace {
 
-struct TreeNode {
-  uint8_t board[kMaxN];
-  uint8_t blank, g, pre, move;  // move: from parent (kNoPre for the root)
-  int32_t parent;
-  int32_t h;
-  int32_t maxf;                 // max of g+h over the path root..this node
-  uint8_t nchild;               // legal non-reverse children
-  uint8_t leaf;                 // 1: root-set member (device task when active)
-  uint8_t pad[2];
+// Root-set template of one blank cell: the tree expanded to a uniform depth
+// D (every node of depth < D expanded, children in move order, no reverse
+// moves), in breadth-first order.  Nodes are move sequences from the root;
+// the device applies them to each instance's board (frontier.cu).
+struct FrontTemplate {
+  bool built = false;
+  uint32_t D = 0;
+  uint32_t node_off = 0;          // first node in the device template arrays
+  std::vector<uint64_t> path;     // 2 bits per move, first move lowest
+  std::vector<int32_t> parent;
+  std::vector<uint8_t> nchild, depth;
+  std::vector<uint32_t> lev;      // level d: nodes [lev[d], lev[d + 1])
 };
 
 struct Instance {
@@ -94,17 +98,17 @@ struct Instance {
   int h0 = 0;
   int iter = 0;
   bool done = false;
-  std::vector<TreeNode> tree;
-  // after h is known: root-set leaves sorted by maxf (the active leaves of a
-  // round are a prefix), interior nodes as (maxf, cumulative children)
-  std::vector<int32_t> leaves;
-  std::vector<int32_t> leaf_maxf;
-  std::vector<uint8_t> leaf_g;       // depth of each leaf, same order
-  std::vector<std::pair<int32_t, uint64_t>> interior;
-  std::vector<int32_t> goals;        // tree nodes with h == 0
+  // root set: the template of the instance's blank cell; its leaves are the
+  // SubRoots [sub_base, sub_base + n_leaves), sorted by maxf (the prefix
+  // maximum of g + h along the path), so a round's active roots are a prefix
+  const FrontTemplate *tmpl = nullptr;
+  uint32_t n_leaves = 0;
+  std::vector<uint32_t> leaf_cum;    // [b]: leaves with maxf <= h0 + b
+  std::vector<uint32_t> goal_key;    // [b]: min (depth << 24 | node) of goal nodes with maxf == h0 + b
+  std::vector<std::pair<int32_t, uint64_t>> interior;  // (maxf, cumulative children), ascending
   std::vector<uint64_t> last_load;   // per leaf, previous round
   uint64_t last_total = 0, prev_total = 0;
-  uint32_t sub_base = 0;             // SubRoot index of leaves[0]
+  uint32_t sub_base = 0;             // SubRoot index of the first leaf
   sp_result *out = nullptr;
 };
 
@@ -153,17 +157,47 @@ struct Pinned {
 
 // Device tables of the multi-iteration mode (grow-only).
 struct MultiBufs {
-  int32_t *iter = nullptr, *fin = nullptr, *status = nullptr, *goal = nullptr, *subf = nullptr, *ifv = nullptr;
+  int32_t *iter = nullptr, *fin = nullptr, *status = nullptr, *goal = nullptr, *ifv = nullptr;
   uint32_t *out = nullptr, *base = nullptr, *nsub = nullptr, *ioff = nullptr, *ilen = nullptr;
   unsigned long long *icum = nullptr, *iter_nodes = nullptr, *loads = nullptr, *fin_ns = nullptr, *t0_ns = nullptr;
   uint8_t *growth = nullptr;  // learned balancer: [n_subs][kGrowthSlacks] growth codes
-  size_t cap_iter = 0, cap_fin = 0, cap_status = 0, cap_goal = 0, cap_subf = 0, cap_ifv = 0, cap_out = 0,
+  size_t cap_iter = 0, cap_fin = 0, cap_status = 0, cap_goal = 0, cap_ifv = 0, cap_out = 0,
          cap_base = 0, cap_nsub = 0, cap_ioff = 0, cap_ilen = 0, cap_icum = 0, cap_iter_nodes = 0, cap_loads = 0,
          cap_fin_ns = 0, cap_t0_ns = 0, cap_growth = 0;
   bool use_growth = false;  // the current launch has growth codes
   void release() {
-    void *ptrs[] = {iter, fin,  status, goal, subf,       ifv,   out,    base,
-                    nsub, ioff, ilen,   icum, iter_nodes, loads, fin_ns, t0_ns, growth};
+    void *ptrs[] = {iter, fin,  status, goal, ifv,        out,   base,   nsub,
+                    ioff, ilen, icum,   iter_nodes, loads, fin_ns, t0_ns, growth};
+    for (void *p : ptrs) cudaFree(p);
+  }
+};
+
+// Device root set: the templates of the current target (one per blank cell,
+// built on first use) and the per-batch outputs of frontier.cu.
+struct FrontBufs {
+  int target = -1;
+  FrontTemplate t[kMaxN];
+  bool dirty = false;  // a template was built since the last upload
+  FrontTmpl *tmpl = nullptr;
+  uint32_t *lev = nullptr;
+  uint64_t *path = nullptr;
+  int32_t *parent = nullptr;
+  uint8_t *nchild = nullptr, *depth = nullptr;
+  size_t cap_tmpl = 0, cap_lev = 0, cap_path = 0, cap_parent = 0, cap_nchild = 0, cap_depth = 0;
+  uint8_t *in = nullptr;  // tiles, then the four per-block arrays
+  int16_t *f = nullptr, *maxf = nullptr;
+  int32_t *leaf_maxf = nullptr, *leaf_node = nullptr, *error = nullptr;
+  uint8_t *leaf_h = nullptr;
+  FrontInst *out = nullptr;
+  size_t cap_in = 0, cap_f = 0, cap_maxf = 0, cap_leaf_maxf = 0, cap_leaf_node = 0, cap_error = 0, cap_leaf_h = 0,
+         cap_out = 0;
+  Pinned<uint8_t> h_in;
+  Pinned<FrontInst> h_out;
+  Pinned<int32_t> h_leaf_node;  // template node of each SubRoot
+  Pinned<uint8_t> h_leaf_h;     // h of each SubRoot (learned balancer)
+  Pinned<int32_t> h_error;
+  void release() {
+    void *ptrs[] = {tmpl, lev, path, parent, nchild, depth, in, f, maxf, leaf_maxf, leaf_node, error, leaf_h, out};
     for (void *p : ptrs) cudaFree(p);
   }
 };
@@ -206,7 +240,7 @@ struct sp_solver {
   int32_t *d_limit = nullptr;
   Solution *d_sol = nullptr;
   size_t inst_cap = 0;
-  uint8_t *d_boards = nullptr;
+  uint8_t *d_boards = nullptr;  // sp_heuristic
   int32_t *d_h = nullptr;
   size_t boards_cap = 0, h_cap = 0;
   // pinned staging
@@ -217,10 +251,10 @@ struct sp_solver {
   Pinned<PoolCtl> h_ctl;
   Pinned<int32_t> h_limits;
   Pinned<uint32_t> h_cnt;
-  Pinned<uint8_t> h_boards;
-  Pinned<int32_t> h_hv;
-  Pinned<SubRoot> h_subs;
+  Pinned<uint8_t> h_stage_up, h_stage_dn;  // solve_multi's tables and results
+  Pinned<unsigned long long> h_loads;
   MultiBufs mb;
+  FrontBufs fb;
   std::unique_ptr<lbm::Model> lbm;  // learned load balancer (SP_LB_LEARNED)
   std::string err;
   sp_stats stats{};
@@ -287,41 +321,6 @@ void build_heur_tables(int w, HeurTables *ht) {
   }
 }
 
-void make_root(int w, const uint8_t *tiles, TreeNode *r) {
-  memset(r, 0, sizeof(*r));
-  const int n = w * w;
-  for (int i = 0; i < n; ++i) {
-    r->board[i] = tiles[i];
-    if (!tiles[i]) r->blank = (uint8_t)i;
-  }
-  r->pre = kNoPre;
-  r->move = kNoPre;
-  r->parent = -1;
-  r->leaf = 1;
-}
-
-// Append the children of tree[idx] (legal, not reversing its move).
-void expand_node(int w, std::vector<TreeNode> &tree, int idx) {
-  const TreeNode p = tree[(size_t)idx];
-  uint32_t mv = legal_moves(w, p.blank);
-  if (p.pre != kNoPre) mv &= ~(1u << (3 - p.pre));
-  for (int d = 0; d < 4; ++d) {
-    if (!((mv >> d) & 1u)) continue;
-    TreeNode c = p;
-    const int src = p.blank + move_delta(w, d);
-    c.board[p.blank] = p.board[src];
-    c.board[src] = 0;
-    c.blank = (uint8_t)src;
-    c.g = (uint8_t)(p.g + 1);
-    c.pre = (uint8_t)d;
-    c.move = (uint8_t)d;
-    c.parent = idx;
-    c.leaf = 1;
-    tree.push_back(c);
-  }
-  tree[(size_t)idx].leaf = 0;
-}
-
 // Host worker threads, created once and kept for the process (never joined:
 // a library must not block at exit on its own threads).  run(n, fn) calls
 // fn(i) for i in [0, n) on the workers and the caller; one run at a time.
@@ -383,10 +382,12 @@ class WorkPool {
 };
 
 // fn(i) for i in [0, n) on the host worker pool (instances are independent);
-// small n runs inline
+// small n, or little total work (`work` elements: waking the workers costs
+// tens of microseconds), runs inline
+constexpr size_t kInlineWork = 16384;
 template <typename F>
-void parallel_for(size_t n, F fn) {
-  if (n < 8 || WorkPool::get().workers() == 0) {
+void parallel_for(size_t n, F fn, size_t work = ~(size_t)0) {
+  if (n < 8 || work < kInlineWork || WorkPool::get().workers() == 0) {
     for (size_t i = 0; i < n; ++i) fn(i);
     return;
   }
@@ -394,96 +395,213 @@ void parallel_for(size_t n, F fn) {
   WorkPool::get().run(n, f);
 }
 
-uint8_t count_children(int w, const TreeNode &t) {
-  uint32_t mv = legal_moves(w, t.blank);
-  if (t.pre != kNoPre) mv &= ~(1u << (3 - t.pre));
-  return (uint8_t)__builtin_popcount(mv);
+// The template of blank cell `blank`: levels expanded while the last level
+// holds fewer than `target` nodes.  Returns false if that needs more than
+// kFrontMaxDepth levels (never for targets up to 2^20).
+bool build_template(int w, int blank, int target, FrontTemplate &T) {
+  T = FrontTemplate{};
+  std::vector<uint8_t> cell{(uint8_t)blank}, pre{kNoPre};
+  T.path.push_back(0);
+  T.parent.push_back(-1);
+  T.depth.push_back(0);
+  T.lev.assign(kFrontLevStride, 0);
+  uint32_t lo = 0, hi = 1, D = 0;
+  while (hi - lo < (uint32_t)target) {
+    if (D >= (uint32_t)kFrontMaxDepth) return false;
+    for (uint32_t x = lo; x < hi; ++x) {
+      uint32_t mv = legal_moves(w, cell[x]);
+      if (pre[x] != kNoPre) mv &= ~(1u << (3 - pre[x]));
+      for (int d = 0; d < 4; ++d) {
+        if (!((mv >> d) & 1u)) continue;
+        T.path.push_back(T.path[x] | ((uint64_t)d << (2 * D)));
+        T.parent.push_back((int32_t)x);
+        T.depth.push_back((uint8_t)(D + 1));
+        cell.push_back((uint8_t)(cell[x] + move_delta(w, d)));
+        pre.push_back((uint8_t)d);
+      }
+    }
+    lo = hi;
+    hi = (uint32_t)T.path.size();
+    T.lev[++D] = lo;
+  }
+  T.lev[D + 1] = hi;
+  T.D = D;
+  T.nchild.resize(hi);
+  for (uint32_t x = 0; x < hi; ++x) {
+    uint32_t mv = legal_moves(w, cell[x]);
+    if (pre[x] != kNoPre) mv &= ~(1u << (3 - pre[x]));
+    T.nchild[x] = x < lo ? (uint8_t)__builtin_popcount(mv) : 0;
+  }
+  T.built = true;
+  return hi < (1u << 24);  // node ids fit the goal keys
 }
 
-// h of every tree node of every instance, on the GPU; then maxf, children,
-// the leaves sorted by maxf and the interior prefix sums.
-int finish_trees(sp_solver *s, std::vector<Instance> &inst) {
-  size_t total = 0;
-  for (auto &I : inst) total += I.tree.size();
-  if (!total) return SP_OK;
-  int rc = ensure(s, &s->d_boards, &s->boards_cap, total * (size_t)s->n);
-  if (rc) return rc;
-  rc = ensure(s, &s->d_h, &s->h_cap, total);
-  if (rc) return rc;
-  Pinned<uint8_t> &boards = s->h_boards;
-  Pinned<int32_t> &hv = s->h_hv;
-  SP_CUDA(s, boards.reserve(total * (size_t)s->n));
-  SP_CUDA(s, hv.reserve(total));
-  std::vector<size_t> first(inst.size() + 1, 0);
-  for (size_t i = 0; i < inst.size(); ++i) first[i + 1] = first[i] + inst[i].tree.size();
-  parallel_for(inst.size(), [&](size_t i) {
-    uint8_t *o = boards.p + first[i] * s->n;
-    if (s->n == 16) {  // fixed sizes: the copies inline
-      for (auto &t : inst[i].tree) memcpy(o, t.board, 16), o += 16;
-    } else {
-      for (auto &t : inst[i].tree) memcpy(o, t.board, 25), o += 25;
-    }
-  });
-  SP_CUDA(s, cudaMemcpyAsync(s->d_boards, boards.p, total * s->n, cudaMemcpyHostToDevice, s->st));
-  s->stats.h2d_bytes += total * s->n;
-  SP_CUDA(s, launch_heuristic(s->w, s->heur == SP_HEUR_PDB, s->d_boards, (int)total, s->d_h, s->d_ht,
-                              s->d_pdb, s->st));
-  SP_CUDA(s, cudaMemcpyAsync(hv.p, s->d_h, total * sizeof(int32_t), cudaMemcpyDeviceToHost, s->st));
-  SP_CUDA(s, cudaStreamSynchronize(s->st));
-  s->stats.d2h_bytes += total * sizeof(int32_t);
-  parallel_for(inst.size(), [&](size_t i) {
+// Root sets of every live instance, built on the device (frontier.cu):
+// templates for this target (built once per blank cell and uploaded when new),
+// one upload of the tiles and the per-instance offsets, one launch, and the
+// per-instance summaries back.  Sets h0, the leaf counts, interior counts and
+// goals of each instance and returns the number of SubRoots.
+int build_root_sets(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst, int target,
+                    size_t *n_subs_out) {
+  FrontBufs &fb = s->fb;
+  const int w = s->w, n = s->n;
+  if (fb.target != target) {
+    for (auto &t : fb.t) t = FrontTemplate{};
+    fb.target = target;
+    fb.dirty = true;
+  }
+  std::vector<uint32_t> live;
+  for (size_t i = 0; i < inst.size(); ++i) {
     Instance &I = inst[i];
-    size_t o = first[i];
-    for (auto &t : I.tree) {
-      t.h = hv.p[o++];
-      const int f = (int)t.g + t.h;
-      t.maxf = t.parent < 0 ? f : std::max(I.tree[(size_t)t.parent].maxf, f);
-      t.nchild = count_children(s->w, t);
-    }
-    if (I.done) return;
-    I.h0 = I.tree[0].h;
-    I.leaves.clear();
-    std::vector<std::pair<int32_t, uint8_t>> interior;
-    for (size_t j = 0; j < I.tree.size(); ++j) {
-      const TreeNode &t = I.tree[j];
-      if (t.leaf) I.leaves.push_back((int32_t)j);
-      else interior.push_back({t.maxf, t.nchild});
-      if (t.h == 0) I.goals.push_back((int32_t)j);
-    }
-    {  // stable counting sort of the leaves by maxf (a small range of integers)
-      int lo = INT32_MAX, hi = INT32_MIN;
-      for (int32_t x : I.leaves) {
-        lo = std::min(lo, I.tree[(size_t)x].maxf);
-        hi = std::max(hi, I.tree[(size_t)x].maxf);
+    if (I.done) continue;
+    int blank = 0;
+    for (int c = 0; c < n; ++c)
+      if (!tiles[i * (size_t)n + c]) blank = c;
+    FrontTemplate &T = fb.t[blank];
+    if (!T.built) {
+      if (!build_template(w, blank, target, T)) {
+        s->err = "root-set template too deep or too large";
+        return SP_ERR_CAPACITY;
       }
-      if (!I.leaves.empty() && hi - lo < 4096) {
-        std::vector<uint32_t> cnt((size_t)(hi - lo) + 2, 0);
-        for (int32_t x : I.leaves) ++cnt[(size_t)(I.tree[(size_t)x].maxf - lo) + 1];
-        for (size_t b = 1; b < cnt.size(); ++b) cnt[b] += cnt[b - 1];
-        std::vector<int32_t> sorted(I.leaves.size());
-        for (int32_t x : I.leaves) sorted[cnt[(size_t)(I.tree[(size_t)x].maxf - lo)]++] = x;
-        I.leaves.swap(sorted);
-      } else {
-        std::stable_sort(I.leaves.begin(), I.leaves.end(),
-                         [&](int32_t a, int32_t b) { return I.tree[(size_t)a].maxf < I.tree[(size_t)b].maxf; });
-      }
+      fb.dirty = true;
     }
-    I.leaf_maxf.resize(I.leaves.size());
-    I.leaf_g.resize(I.leaves.size());
-    for (size_t q = 0; q < I.leaves.size(); ++q) {
-      I.leaf_maxf[q] = I.tree[(size_t)I.leaves[q]].maxf;
-      I.leaf_g[q] = I.tree[(size_t)I.leaves[q]].g;
+    I.tmpl = &T;
+    live.push_back((uint32_t)i);
+  }
+  int rc = SP_OK;
+  if (fb.dirty) {  // all built templates, concatenated
+    size_t nodes = 0;
+    for (auto &t : fb.t)
+      if (t.built) t.node_off = (uint32_t)nodes, nodes += t.path.size();
+    if ((rc = ensure(s, &fb.tmpl, &fb.cap_tmpl, (size_t)kMaxN)) ||
+        (rc = ensure(s, &fb.lev, &fb.cap_lev, (size_t)kMaxN * kFrontLevStride)) ||
+        (rc = ensure(s, &fb.path, &fb.cap_path, nodes)) || (rc = ensure(s, &fb.parent, &fb.cap_parent, nodes)) ||
+        (rc = ensure(s, &fb.nchild, &fb.cap_nchild, nodes)) || (rc = ensure(s, &fb.depth, &fb.cap_depth, nodes)))
+      return rc;
+    std::vector<FrontTmpl> desc(kMaxN, FrontTmpl{});
+    std::vector<uint32_t> lev((size_t)kMaxN * kFrontLevStride, 0);
+    std::vector<uint64_t> path(nodes);
+    std::vector<int32_t> parent(nodes);
+    std::vector<uint8_t> nchild(nodes), depth(nodes);
+    for (int b = 0; b < kMaxN; ++b) {
+      const FrontTemplate &t = fb.t[b];
+      if (!t.built) continue;
+      desc[b] = FrontTmpl{t.node_off, (uint32_t)t.path.size(), t.D, 0};
+      std::copy(t.lev.begin(), t.lev.end(), lev.begin() + (size_t)b * kFrontLevStride);
+      std::copy(t.path.begin(), t.path.end(), path.begin() + t.node_off);
+      std::copy(t.parent.begin(), t.parent.end(), parent.begin() + t.node_off);
+      std::copy(t.nchild.begin(), t.nchild.end(), nchild.begin() + t.node_off);
+      std::copy(t.depth.begin(), t.depth.end(), depth.begin() + t.node_off);
     }
-    std::sort(interior.begin(), interior.end());
+    SP_CUDA(s, cudaMemcpy(fb.tmpl, desc.data(), desc.size() * sizeof(FrontTmpl), cudaMemcpyHostToDevice));
+    SP_CUDA(s, cudaMemcpy(fb.lev, lev.data(), lev.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    SP_CUDA(s, cudaMemcpy(fb.path, path.data(), nodes * sizeof(uint64_t), cudaMemcpyHostToDevice));
+    SP_CUDA(s, cudaMemcpy(fb.parent, parent.data(), nodes * sizeof(int32_t), cudaMemcpyHostToDevice));
+    SP_CUDA(s, cudaMemcpy(fb.nchild, nchild.data(), nodes, cudaMemcpyHostToDevice));
+    SP_CUDA(s, cudaMemcpy(fb.depth, depth.data(), nodes, cudaMemcpyHostToDevice));
+    fb.dirty = false;
+  }
+  // per live instance: template, first SubRoot, first scratch node
+  const size_t nl = live.size();
+  size_t n_subs = 0, n_nodes = 0;
+  std::vector<uint32_t> arr(4 * std::max<size_t>(nl, 1), 0);
+  for (size_t k = 0; k < nl; ++k) {
+    Instance &I = inst[live[k]];
+    const FrontTemplate &T = *I.tmpl;
+    I.sub_base = (uint32_t)n_subs;
+    I.n_leaves = T.lev[T.D + 1] - T.lev[T.D];
+    arr[k] = live[k];
+    arr[nl + k] = (uint32_t)(&T - fb.t);
+    arr[2 * nl + k] = (uint32_t)n_subs;
+    arr[3 * nl + k] = (uint32_t)n_nodes;
+    n_subs += I.n_leaves;
+    n_nodes += T.path.size();
+  }
+  *n_subs_out = n_subs;
+  if ((rc = ensure(s, &s->d_subs, &s->subs_cap, std::max<size_t>(n_subs, 1))) ||
+      (rc = ensure(s, &s->d_sub_nodes, &s->sub_nodes_cap, std::max<size_t>(n_subs, 1))))
+    return rc;
+  if (!nl) return SP_OK;
+  if (n_subs > 0xFFFFFFF0ull || n_nodes > 0xFFFFFFF0ull) {
+    s->err = "root set too large";
+    return SP_ERR_CAPACITY;
+  }
+  const size_t tiles_bytes = (inst.size() * (size_t)n + 15) & ~(size_t)15;
+  const size_t in_bytes = tiles_bytes + 4 * nl * sizeof(uint32_t);
+  if ((rc = ensure(s, &fb.in, &fb.cap_in, in_bytes)) || (rc = ensure(s, &fb.f, &fb.cap_f, n_nodes)) ||
+      (rc = ensure(s, &fb.maxf, &fb.cap_maxf, n_nodes)) ||
+      (rc = ensure(s, &fb.leaf_maxf, &fb.cap_leaf_maxf, n_subs)) ||
+      (rc = ensure(s, &fb.leaf_node, &fb.cap_leaf_node, n_subs)) ||
+      (rc = ensure(s, &fb.leaf_h, &fb.cap_leaf_h, n_subs)) || (rc = ensure(s, &fb.out, &fb.cap_out, nl)) ||
+      (rc = ensure(s, &fb.error, &fb.cap_error, (size_t)1)))
+    return rc;
+  SP_CUDA(s, fb.h_in.reserve(in_bytes));
+  SP_CUDA(s, fb.h_out.reserve(nl));
+  SP_CUDA(s, fb.h_error.reserve(1));
+  memcpy(fb.h_in.p, tiles, inst.size() * (size_t)n);
+  memcpy(fb.h_in.p + tiles_bytes, arr.data(), 4 * nl * sizeof(uint32_t));
+  SP_CUDA(s, cudaMemcpyAsync(fb.in, fb.h_in.p, in_bytes, cudaMemcpyHostToDevice, s->st));
+  SP_CUDA(s, cudaMemsetAsync(fb.error, 0, sizeof(int32_t), s->st));
+  s->stats.h2d_bytes += in_bytes;
+  const uint32_t *d_arr = reinterpret_cast<const uint32_t *>(fb.in + tiles_bytes);
+  FrontArgs A{};
+  A.tiles = fb.in;
+  A.live = d_arr;
+  A.live_tmpl = d_arr + nl;
+  A.live_base = d_arr + 2 * nl;
+  A.live_scratch = d_arr + 3 * nl;
+  A.tmpl = fb.tmpl;
+  A.lev = fb.lev;
+  A.path = fb.path;
+  A.parent = fb.parent;
+  A.nchild = fb.nchild;
+  A.depth = fb.depth;
+  A.ht = s->d_ht;
+  A.pdb = s->d_pdb;
+  A.f = fb.f;
+  A.maxf = fb.maxf;
+  A.subs = s->d_subs;
+  A.leaf_maxf = fb.leaf_maxf;
+  A.leaf_h = fb.leaf_h;
+  A.leaf_node = fb.leaf_node;
+  A.out = fb.out;
+  A.error = fb.error;
+  SP_CUDA(s, launch_frontier(w, s->heur == SP_HEUR_PDB, (int)nl, A, s->st));
+  s->stats.kernel_launches += 1;
+  SP_CUDA(s, cudaMemcpyAsync(fb.h_out.p, fb.out, nl * sizeof(FrontInst), cudaMemcpyDeviceToHost, s->st));
+  SP_CUDA(s, cudaMemcpyAsync(fb.h_error.p, fb.error, sizeof(int32_t), cudaMemcpyDeviceToHost, s->st));
+  SP_CUDA(s, cudaStreamSynchronize(s->st));
+  s->stats.d2h_bytes += nl * sizeof(FrontInst) + sizeof(int32_t);
+  if (*fb.h_error.p) {
+    s->err = "root set: the heuristic changes by more than the bucket range allows along a path";
+    return *fb.h_error.p;
+  }
+  // template node and h of every SubRoot: read by the host only after later
+  // synchronisations (solution paths, the learned balancer)
+  SP_CUDA(s, fb.h_leaf_node.reserve(n_subs));
+  SP_CUDA(s, cudaMemcpyAsync(fb.h_leaf_node.p, fb.leaf_node, n_subs * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                             s->st));
+  s->stats.d2h_bytes += n_subs * sizeof(int32_t);
+  if (s->cfg.lb_mode == SP_LB_LEARNED) {
+    SP_CUDA(s, fb.h_leaf_h.reserve(n_subs));
+    SP_CUDA(s, cudaMemcpyAsync(fb.h_leaf_h.p, fb.leaf_h, n_subs, cudaMemcpyDeviceToHost, s->st));
+    s->stats.d2h_bytes += n_subs;
+  }
+  for (size_t k = 0; k < nl; ++k) {
+    Instance &I = inst[live[k]];
+    const FrontInst &O = fb.h_out.p[k];
+    I.h0 = O.h0;
+    I.leaf_cum.assign(O.leaf_cum, O.leaf_cum + kFrontBuckets);
+    I.goal_key.assign(O.goal, O.goal + kFrontBuckets);
     I.interior.clear();
     uint64_t cum = 0;
-    for (auto &x : interior) {
-      cum += x.second;
-      if (!I.interior.empty() && I.interior.back().first == x.first) I.interior.back().second = cum;
-      else I.interior.push_back({x.first, cum});
+    for (uint32_t b = 0; b < (uint32_t)kFrontBuckets; ++b) {
+      if (!O.child[b]) continue;
+      cum += O.child[b];
+      I.interior.push_back({I.h0 + (int32_t)b, cum});
     }
-    I.last_load.assign(I.leaves.size(), 0);
-  });
+    I.last_load.assign(I.n_leaves, 0);
+  }
   return SP_OK;
 }
 
@@ -495,7 +613,8 @@ uint64_t interior_nodes(const Instance &I, int L) {
 }
 
 size_t active_leaves(const Instance &I, int L) {
-  return (size_t)(std::upper_bound(I.leaf_maxf.begin(), I.leaf_maxf.end(), L) - I.leaf_maxf.begin());
+  if (L < I.h0) return 0;
+  return L - I.h0 >= kFrontBuckets ? I.n_leaves : I.leaf_cum[(size_t)(L - I.h0)];
 }
 
 bool replay_ok(int w, const uint8_t *tiles, const uint8_t *moves, int len) {
@@ -656,7 +775,7 @@ int launch_round(sp_solver *s, const RoundPlan &plan, size_t n_subs, size_t n_in
     P.inst_status = m.status;
     P.inst_sub_base = m.base;
     P.inst_nsub = m.nsub;
-    P.sub_maxf = m.subf;
+    P.sub_maxf = s->fb.leaf_maxf;
     P.inter_off = m.ioff;
     P.inter_len = m.ilen;
     P.inter_f = m.ifv;
@@ -719,9 +838,12 @@ int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int3
   const size_t nc = off[ni];
   if (!stat) {
     plan.direct.resize(nc);
-    parallel_for(ni, [&](size_t i) {
-      for (size_t q = 0; q < off[i + 1] - off[i]; ++q) plan.direct[off[i] + q] = inst[i].sub_base + (uint32_t)q;
-    });
+    parallel_for(
+        ni,
+        [&](size_t i) {
+          for (size_t q = 0; q < off[i + 1] - off[i]; ++q) plan.direct[off[i] + q] = inst[i].sub_base + (uint32_t)q;
+        },
+        nc);
     return SP_OK;
   }
   std::vector<double> pred(nc), inst_total(ni, 0.0);
@@ -739,11 +861,11 @@ int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int3
       const double p = (double)I.last_load[q] * growth;
       pred[off[i] + q] = p;
       csub[off[i] + q] = I.sub_base + (uint32_t)q;
-      room[off[i] + q] = (int16_t)(limits[i] - (int)I.leaf_g[q]);
+      room[off[i] + q] = (int16_t)(limits[i] - (int)I.tmpl->D);
       tot += p;
     }
     inst_total[i] = tot;
-  });
+  }, nc);
   double total = 0;
   for (double t : inst_total) total += t;
   if (learned && nc) {
@@ -760,8 +882,8 @@ int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int3
     for (size_t i = 0; i < ni; ++i) {
       const Instance &I = inst[i];
       for (size_t q = 0; q < off[i + 1] - off[i]; ++q) {
-        const TreeNode &t = I.tree[(size_t)I.leaves[q]];
-        const int sl = std::min(kLbmMaxSlack, std::max(0, (limits[i] - (int)t.g - t.h) / 2));
+        const int leaf_h = s->fb.h_leaf_h.p[I.sub_base + q];
+        const int sl = std::min(kLbmMaxSlack, std::max(0, (limits[i] - (int)I.tmpl->D - leaf_h) / 2));
         q_sub.push_back(I.sub_base + (uint32_t)q);
         q_slack.push_back(sl);
         if (I.last_load[q]) {
@@ -883,18 +1005,20 @@ int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int3
 
 // Result path of a solved instance: the root-set tree prefix to its goal (a
 // tree node) or to the device solution's root, then the device's moves.
-void set_path(int w, Instance &I, const uint8_t *tiles, int host_goal, const Solution *sol) {
+// `leaf_node` maps a SubRoot to its template node.
+void set_path(int w, Instance &I, const uint8_t *tiles, int host_goal, const Solution *sol,
+              const int32_t *leaf_node) {
   std::vector<uint8_t> mv;
   int node = host_goal;
   uint32_t extra = 0;
   const uint32_t *pw = nullptr;
   if (node < 0) {
-    node = I.leaves[sol->sub - I.sub_base];
+    node = leaf_node[sol->sub];
     extra = sol->len;
     pw = sol->path;
   }
-  for (int x = node; x > 0; x = I.tree[(size_t)x].parent) mv.push_back(I.tree[(size_t)x].move);
-  std::reverse(mv.begin(), mv.end());
+  const FrontTemplate &T = *I.tmpl;
+  for (int j = 0; j < T.depth[(size_t)node]; ++j) mv.push_back((uint8_t)((T.path[(size_t)node] >> (2 * j)) & 3u));
   for (uint32_t j = 0; j < extra; ++j) mv.push_back((uint8_t)((pw[j >> 4] >> (2 * (j & 15))) & 3u));
   sp_result *R = I.out;
   R->len = (int32_t)mv.size();
@@ -907,13 +1031,19 @@ void set_path(int w, Instance &I, const uint8_t *tiles, int host_goal, const Sol
   }
 }
 
+// The shallowest root-set goal node (first in tree order) whose path stays
+// within L, or -1.
 int tree_goal(const Instance &I, int L) {
-  int best = -1;
-  for (int32_t x : I.goals) {
-    const TreeNode &t = I.tree[(size_t)x];
-    if (t.maxf <= L && (best < 0 || t.g < I.tree[(size_t)best].g)) best = x;
-  }
-  return best;
+  uint32_t best = 0xFFFFFFFFu;
+  for (int b = 0; b < kFrontBuckets && I.h0 + b <= L; ++b) best = std::min(best, I.goal_key[(size_t)b]);
+  return best == 0xFFFFFFFFu ? -1 : (int)(best & 0xFFFFFFu);
+}
+
+// Smallest maxf of a root-set goal node (INT32_MAX: none).
+int32_t goal_maxf(const Instance &I) {
+  for (int b = 0; b < kFrontBuckets; ++b)
+    if (I.goal_key[(size_t)b] != 0xFFFFFFFFu) return I.h0 + b;
+  return 0x7FFFFFFF;
 }
 
 // Multi-iteration mode: every instance's threshold loop runs on the device in
@@ -926,22 +1056,21 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
   const int w = s->w, n = s->n;
   std::vector<int32_t> h_iter(ni, 0), h_limit(ni, 0), h_final(ni, -1), h_goal(ni, 0x7FFFFFFF);
   std::vector<uint32_t> h_out(ni, 0), h_base(ni, 0), h_nsub(ni, 0), h_ioff(ni, 0), h_ilen(ni, 0);
-  std::vector<int32_t> h_subf(std::max<size_t>(n_subs, 1), 0x7FFFFFFF), h_if;
+  std::vector<int32_t> h_if;
   std::vector<unsigned long long> h_icum;
   std::vector<uint32_t> direct;
   for (size_t i = 0; i < ni; ++i) {
     Instance &I = inst[i];
     h_base[i] = I.sub_base;
     if (I.done) continue;
-    for (int32_t x : I.goals) h_goal[i] = std::min(h_goal[i], I.tree[(size_t)x].maxf);
+    h_goal[i] = goal_maxf(I);
     h_ioff[i] = (uint32_t)h_if.size();
     h_ilen[i] = (uint32_t)I.interior.size();
     for (auto &e : I.interior) {
       h_if.push_back(e.first);
       h_icum.push_back(e.second);
     }
-    for (size_t q = 0; q < I.leaves.size(); ++q) h_subf[I.sub_base + q] = I.leaf_maxf[q];
-    h_nsub[i] = (uint32_t)I.leaves.size();
+    h_nsub[i] = I.n_leaves;
     // iterations without any active leaf: the root-set tree holds them whole
     int L = I.h0;
     for (;;) {
@@ -962,7 +1091,7 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
       R->n_iter = I.iter + 1;
       const int hg = tree_goal(I, L);
       if (hg >= 0) {
-        set_path(w, I, tiles + i * (size_t)n, hg, nullptr);
+        set_path(w, I, tiles + i * (size_t)n, hg, nullptr, s->fb.h_leaf_node.p);
         I.done = true;
         break;
       }
@@ -985,14 +1114,25 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
       (rc = ensure(s, &m.fin, &m.cap_fin, ni)) || (rc = ensure(s, &m.status, &m.cap_status, ni)) ||
       (rc = ensure(s, &m.base, &m.cap_base, ni)) || (rc = ensure(s, &m.nsub, &m.cap_nsub, ni)) ||
       (rc = ensure(s, &m.ioff, &m.cap_ioff, ni)) || (rc = ensure(s, &m.ilen, &m.cap_ilen, ni)) ||
-      (rc = ensure(s, &m.goal, &m.cap_goal, ni)) || (rc = ensure(s, &m.subf, &m.cap_subf, h_subf.size())) ||
+      (rc = ensure(s, &m.goal, &m.cap_goal, ni)) ||
       (rc = ensure(s, &m.ifv, &m.cap_ifv, h_if.size())) || (rc = ensure(s, &m.icum, &m.cap_icum, h_icum.size())) ||
       (rc = ensure(s, &m.iter_nodes, &m.cap_iter_nodes, ni * kMaxIters)) ||
       (rc = ensure(s, &m.loads, &m.cap_loads, 2 * std::max<size_t>(n_subs, 1))) ||
       (rc = ensure(s, &m.fin_ns, &m.cap_fin_ns, ni)) || (rc = ensure(s, &m.t0_ns, &m.cap_t0_ns, 1)))
     return rc;
+  // uploads through one pinned staging buffer (asynchronous copies)
+  auto bytes16 = [](const auto &v) { return (v.size() * sizeof(v[0]) + 15) & ~(size_t)15; };
+  const size_t stage_bytes = bytes16(h_iter) + bytes16(h_limit) + bytes16(h_out) + bytes16(h_final) +
+                             bytes16(h_base) + bytes16(h_nsub) + bytes16(h_ioff) + bytes16(h_ilen) +
+                             bytes16(h_goal) + bytes16(h_if) + bytes16(h_icum) + n_subs * kGrowthSlacks + 16;
+  SP_CUDA(s, s->h_stage_up.reserve(stage_bytes));
+  size_t stage_off = 0;
   auto up = [&](auto *dst, const auto &v) {
-    return cudaMemcpyAsync(dst, v.data(), v.size() * sizeof(v[0]), cudaMemcpyHostToDevice, s->st);
+    const size_t b = v.size() * sizeof(v[0]);
+    uint8_t *src = s->h_stage_up.p + stage_off;
+    memcpy(src, v.data(), b);
+    stage_off += (b + 15) & ~(size_t)15;
+    return cudaMemcpyAsync(dst, src, b, cudaMemcpyHostToDevice, s->st);
   };
   SP_CUDA(s, up(m.iter, h_iter));
   SP_CUDA(s, up(s->d_limit, h_limit));
@@ -1004,7 +1144,6 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
   SP_CUDA(s, up(m.ioff, h_ioff));
   SP_CUDA(s, up(m.ilen, h_ilen));
   SP_CUDA(s, up(m.goal, h_goal));
-  SP_CUDA(s, up(m.subf, h_subf));
   SP_CUDA(s, up(m.ifv, h_if));
   SP_CUDA(s, up(m.icum, h_icum));
   SP_CUDA(s, cudaMemsetAsync(m.iter_nodes, 0, ni * kMaxIters * sizeof(unsigned long long), s->st));
@@ -1046,7 +1185,7 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
     s->stats.h2d_bytes += code.size();
     m.use_growth = true;
   }
-  s->stats.h2d_bytes += ni * 40 + h_subf.size() * 4 + h_if.size() * 12;
+  s->stats.h2d_bytes += ni * 40 + h_if.size() * 12;
   const double pre_s = ms_since(t_start) / 1000.0;  // host part before the launch
   for (auto &I : inst)
     if (I.done) I.out->seconds = pre_s;
@@ -1076,19 +1215,25 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
       return ctl.error;
     }
   }
-  std::vector<int32_t> fin(ni), st(ni);
-  std::vector<unsigned long long> itn(ni * kMaxIters), fin_ns(ni), t0(1, 0);
-  SP_CUDA(s, cudaMemcpyAsync(fin_ns.data(), m.fin_ns, ni * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s->st));
-  SP_CUDA(s, cudaMemcpyAsync(t0.data(), m.t0_ns, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s->st));
-  SP_CUDA(s, cudaMemcpyAsync(fin.data(), m.fin, ni * sizeof(int32_t), cudaMemcpyDeviceToHost, s->st));
-  SP_CUDA(s, cudaMemcpyAsync(st.data(), m.status, ni * sizeof(int32_t), cudaMemcpyDeviceToHost, s->st));
-  SP_CUDA(s, cudaMemcpyAsync(itn.data(), m.iter_nodes, itn.size() * sizeof(unsigned long long),
+  // results through one pinned staging buffer
+  SP_CUDA(s, s->h_stage_dn.reserve(ni * (2 * sizeof(unsigned long long) + 2 * sizeof(int32_t) +
+                                         kMaxIters * sizeof(unsigned long long)) + 64));
+  unsigned long long *fin_ns = reinterpret_cast<unsigned long long *>(s->h_stage_dn.p);
+  unsigned long long *t0 = fin_ns + ni;
+  unsigned long long *itn = t0 + 1;
+  int32_t *fin = reinterpret_cast<int32_t *>(itn + ni * kMaxIters);
+  int32_t *st = fin + ni;
+  SP_CUDA(s, cudaMemcpyAsync(fin_ns, m.fin_ns, ni * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s->st));
+  SP_CUDA(s, cudaMemcpyAsync(t0, m.t0_ns, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s->st));
+  SP_CUDA(s, cudaMemcpyAsync(fin, m.fin, ni * sizeof(int32_t), cudaMemcpyDeviceToHost, s->st));
+  SP_CUDA(s, cudaMemcpyAsync(st, m.status, ni * sizeof(int32_t), cudaMemcpyDeviceToHost, s->st));
+  SP_CUDA(s, cudaMemcpyAsync(itn, m.iter_nodes, ni * kMaxIters * sizeof(unsigned long long),
                              cudaMemcpyDeviceToHost, s->st));
   SP_CUDA(s, cudaStreamSynchronize(s->st));
   s->stats.d2h_bytes += ni * (8 + kMaxIters * 8);
   const Solution *sols = s->h_sols.p;
   int rounds = 0;
-  std::vector<unsigned long long> loads;
+  const unsigned long long *loads = nullptr;
   for (size_t i = 0; i < ni; ++i) {
     Instance &I = inst[i];
     if (I.done) {
@@ -1113,16 +1258,19 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
       // continue in the round loop from iteration fin + 1 with the loads the
       // device measured in iteration fin
       R->seconds = 0.0;
-      if (loads.empty()) {
-        loads.resize(2 * std::max<size_t>(n_subs, 1));
-        SP_CUDA(s, cudaMemcpy(loads.data(), m.loads, loads.size() * sizeof(unsigned long long),
-                              cudaMemcpyDeviceToHost));
-        s->stats.d2h_bytes += loads.size() * sizeof(unsigned long long);
+      if (!loads) {
+        const size_t nl = 2 * std::max<size_t>(n_subs, 1);
+        SP_CUDA(s, s->h_loads.reserve(nl));
+        SP_CUDA(s, cudaMemcpyAsync(s->h_loads.p, m.loads, nl * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                   s->st));
+        SP_CUDA(s, cudaStreamSynchronize(s->st));
+        s->stats.d2h_bytes += nl * sizeof(unsigned long long);
+        loads = s->h_loads.p;
       }
       const int f = fin[i];
-      const unsigned long long *lf = loads.data() + (size_t)(f & 1) * n_subs + I.sub_base;
+      const unsigned long long *lf = loads + (size_t)(f & 1) * n_subs + I.sub_base;
       uint64_t tot = 0;
-      for (size_t q = 0; q < I.leaves.size(); ++q) {
+      for (size_t q = 0; q < I.n_leaves; ++q) {
         I.last_load[q] = lf[q];
         tot += lf[q];
       }
@@ -1139,7 +1287,7 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
     } else {
       const int L = I.h0 + 2 * fin[i];
       const int hg = tree_goal(I, L);
-      set_path(w, I, tiles + i * (size_t)n, hg, hg < 0 ? &sols[i] : nullptr);
+      set_path(w, I, tiles + i * (size_t)n, hg, hg < 0 ? &sols[i] : nullptr, s->fb.h_leaf_node.p);
     }
     I.done = true;
   }
@@ -1175,72 +1323,20 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
       I.out->status = I.status;
       continue;
     }
-    TreeNode root;
-    make_root(w, tiles + (size_t)i * n, &root);
-    I.tree.push_back(root);
   }
-  // root set: uniform-depth tree expansion to >= frontier_target leaves,
-  // instances spread over host threads
+  // root set: uniform-depth tree expansion to >= frontier_target leaves per
+  // instance, on the device
   auto t_front = std::chrono::steady_clock::now();
   // a batch's root set is capped near 8 roots per resident lane: more roots
-  // than that add host work and no balance (donation splits what is left)
+  // than that add work and no balance (donation splits what is left)
   size_t live = 0;
   for (auto &I : inst) live += !I.done;
   const double lanes = s->last_lanes > 0 ? (double)s->last_lanes : (double)s->num_sms * 768.0;
   int target = std::max(1, s->cfg.frontier_target);
   if (live) target = std::min(target, std::max(32, (int)(8.0 * lanes / (double)live)));
-  auto build_tree = [&](Instance &I) {
-    if (I.done) return;
-    I.tree.reserve((size_t)target * 4 + 16);
-    std::vector<int32_t> level{0}, next;
-    level.reserve((size_t)target * 4);
-    next.reserve((size_t)target * 4);
-    for (int dep = 0; dep < 40 && (int)level.size() < target; ++dep) {
-      next.clear();
-      for (int32_t x : level) {
-        const size_t before = I.tree.size();
-        expand_node(w, I.tree, x);
-        for (size_t c = before; c < I.tree.size(); ++c) next.push_back((int32_t)c);
-      }
-      level.swap(next);
-    }
-  };
-  parallel_for(inst.size(), [&](size_t i) { build_tree(inst[i]); });
-  int rc = finish_trees(s, inst);
-  if (rc) return rc;
-  // SubRoot array: the leaves of every instance, in maxf order
   size_t n_subs = 0;
-  for (size_t i = 0; i < inst.size(); ++i) {
-    Instance &I = inst[i];
-    I.sub_base = (uint32_t)n_subs;
-    if (!I.done) n_subs += I.leaves.size();
-  }
-  rc = ensure(s, &s->d_subs, &s->subs_cap, std::max<size_t>(n_subs, 1));
+  int rc = build_root_sets(s, tiles, inst, target, &n_subs);
   if (rc) return rc;
-  rc = ensure(s, &s->d_sub_nodes, &s->sub_nodes_cap, std::max<size_t>(n_subs, 1));
-  if (rc) return rc;
-  if (n_subs) {
-    Pinned<SubRoot> &hs = s->h_subs;
-    SP_CUDA(s, hs.reserve(n_subs));
-    parallel_for(inst.size(), [&](size_t i) {
-      const Instance &I = inst[i];
-      if (I.done) return;
-      SubRoot *out = hs.p + I.sub_base;
-      for (int32_t x : I.leaves) {
-        const TreeNode &t = I.tree[(size_t)x];
-        SubRoot r{};
-        memcpy(r.board, t.board, (size_t)n);
-        r.blank = t.blank;
-        r.g = t.g;
-        r.pre = t.pre;
-        r.inst = (uint32_t)i;
-        *out++ = r;
-      }
-    });
-    SP_CUDA(s, cudaMemcpyAsync(s->d_subs, hs.p, n_subs * sizeof(SubRoot), cudaMemcpyHostToDevice, s->st));
-    SP_CUDA(s, cudaStreamSynchronize(s->st));
-    s->stats.h2d_bytes += n_subs * sizeof(SubRoot);
-  }
   if (inst.size() > s->inst_cap || !s->d_limit) {
     if (s->d_limit) cudaFree(s->d_limit);
     if (s->d_sol) cudaFree(s->d_sol);
@@ -1312,6 +1408,9 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
     ++s->stats.rounds;
     // fold results: per-root loads (parallel over instances), then the rest
     std::vector<uint64_t> dev_nodes(inst.size(), 0);
+    size_t fold_work = 0;
+    for (size_t i = 0; i < inst.size(); ++i)
+      if (!inst[i].done) fold_work += active_leaves(inst[i], limits[i]);
     parallel_for(inst.size(), [&](size_t i) {
       Instance &I = inst[i];
       if (I.done) return;
@@ -1323,7 +1422,7 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
         I.last_load[q] = v;
       }
       dev_nodes[i] = dev;
-    });
+    }, fold_work);
     for (size_t i = 0; i < inst.size(); ++i) {
       Instance &I = inst[i];
       if (I.done) continue;
@@ -1339,34 +1438,11 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
       R->n_iter = I.iter + 1;
       s->stats.nodes += nodes;
       s->stats.round_nodes[ri] += nodes;
-      int host_goal = -1;
-      for (int32_t x : I.goals) {
-        const TreeNode &t = I.tree[(size_t)x];
-        if (t.maxf <= L && (host_goal < 0 || t.g < I.tree[(size_t)host_goal].g)) host_goal = x;
-      }
+      const int host_goal = tree_goal(I, L);
       const bool dev_goal = sols && sols[i].flag != 0;
       if (host_goal >= 0 || dev_goal) {
         // path: root-set tree prefix, then the device's moves below its root
-        std::vector<uint8_t> mv;
-        int node = host_goal;
-        uint32_t extra = 0;
-        const uint32_t *pw = nullptr;
-        if (node < 0) {
-          node = I.leaves[sols[i].sub - I.sub_base];
-          extra = sols[i].len;
-          pw = sols[i].path;
-        }
-        for (int x = node; x > 0; x = I.tree[(size_t)x].parent) mv.push_back(I.tree[(size_t)x].move);
-        std::reverse(mv.begin(), mv.end());
-        for (uint32_t j = 0; j < extra; ++j) mv.push_back((uint8_t)((pw[j >> 4] >> (2 * (j & 15))) & 3u));
-        R->len = (int32_t)mv.size();
-        if (mv.size() > SP_MAX_MOVES) {
-          R->status = SP_ERR_PATH;
-        } else {
-          R->n_moves = R->len;
-          memcpy(R->moves, mv.data(), mv.size());
-          R->status = replay_ok(w, tiles + i * (size_t)n, R->moves, R->n_moves) ? SP_OK : SP_ERR_PATH;
-        }
+        set_path(w, I, tiles + i * (size_t)n, host_goal, host_goal < 0 ? &sols[i] : nullptr, s->fb.h_leaf_node.p);
         I.done = true;
         continue;
       }
@@ -1477,6 +1553,7 @@ void sp_destroy(sp_solver *s) {
   cudaFree(s->d_split_b);
   cudaFree(s->d_emit);
   s->mb.release();
+  s->fb.release();
   if (s->ev0) cudaEventDestroy(s->ev0);
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->st) cudaStreamDestroy(s->st);

@@ -87,6 +87,51 @@ struct SplitArgs {
 };
 cudaError_t launch_split_level(int w, bool pdb, int num_sms, const SplitArgs &A, cudaStream_t st);
 
+// Root-set templates and the device root-set build (frontier.cu).  A
+// template is the uniform-depth tree of one blank cell in breadth-first
+// order; its nodes live at [node_off, node_off + n_nodes) of the template
+// arrays and its level d at [lev[d], lev[d + 1]) (template-relative).
+constexpr int kFrontMaxDepth = 32;                  // moves in a 64-bit path
+constexpr int kFrontLevStride = kFrontMaxDepth + 2;
+// maxf - h0 in [0, 256).  The PDB tables are not consistent: h moved by up
+// to 5 per move over the root sets of the benchmark workloads (maxf - h0 at
+// most 22 at D = 10); 256 leaves room for 6 D at the deepest template.  A
+// larger spread is reported as SP_ERR_ARG.
+constexpr int kFrontBuckets = 256;
+struct FrontTmpl {
+  uint32_t node_off, n_nodes, D, pad;
+};
+struct FrontInst {
+  int32_t h0;
+  uint32_t n_leaves;
+  uint32_t leaf_cum[kFrontBuckets];  // leaves with maxf <= h0 + b
+  uint32_t child[kFrontBuckets];     // children of interior nodes with maxf == h0 + b
+  uint32_t goal[kFrontBuckets];      // min (depth << 24 | node) of goal nodes with maxf == h0 + b
+};
+struct FrontArgs {
+  const uint8_t *tiles;          // [instance][N]
+  const uint32_t *live;          // [block] instance of the block
+  const uint32_t *live_tmpl;     // [block] its template
+  const uint32_t *live_base;     // [block] SubRoot index of its first leaf
+  const uint32_t *live_scratch;  // [block] offset of its nodes in f / maxf
+  const FrontTmpl *tmpl;
+  const uint32_t *lev;           // [template][kFrontLevStride]
+  const uint64_t *path;          // moves from the root, 2 bits each, first move lowest
+  const int32_t *parent;
+  const uint8_t *nchild;
+  const uint8_t *depth;
+  const HeurTables *ht;
+  const uint8_t *pdb;
+  int16_t *f, *maxf;             // scratch, one entry per node
+  SubRoot *subs;                 // leaves, sorted by maxf per instance
+  int32_t *leaf_maxf;
+  uint8_t *leaf_h;
+  int32_t *leaf_node;            // template node of each SubRoot
+  FrontInst *out;                // [block]
+  int32_t *error;
+};
+cudaError_t launch_frontier(int w, bool pdb, int n_live, const FrontArgs &A, cudaStream_t st);
+
 // h of n boards (n * N bytes) into h[n]; PDB tables as in RoundParams.
 cudaError_t launch_heuristic(int w, bool pdb, const uint8_t *boards, int n, int32_t *h,
                              const HeurTables *ht, const uint8_t *tables, cudaStream_t st);
