@@ -836,38 +836,42 @@ int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int3
   for (size_t i = 0; i < ni; ++i)
     off[i + 1] = off[i] + (inst[i].done ? 0 : active_leaves(inst[i], limits[i]));
   const size_t nc = off[ni];
+  // candidate chunks for the worker pool; chunk c starts in instance c_inst[c]
+  const size_t nchunk = std::max<size_t>(1, std::min<size_t>(128, nc / 2048));
+  auto chunk_lo = [&](size_t c) { return nc * c / nchunk; };
+  std::vector<size_t> c_inst(nchunk, 0);
+  for (size_t c = 0; c < nchunk; ++c)
+    c_inst[c] = (size_t)(std::upper_bound(off.begin(), off.end(), chunk_lo(c)) - off.begin()) - 1;
+  // calls fn(j, i, q) for the candidates j of chunk c: root q of instance i
+  auto for_chunk = [&](size_t c, auto fn) {
+    size_t i = c_inst[c];
+    for (size_t j = chunk_lo(c); j < chunk_lo(c + 1); ++j) {
+      while (j >= off[i + 1]) ++i;
+      fn(j, i, j - off[i]);
+    }
+  };
   if (!stat) {
     plan.direct.resize(nc);
-    parallel_for(
-        ni,
-        [&](size_t i) {
-          for (size_t q = 0; q < off[i + 1] - off[i]; ++q) plan.direct[off[i] + q] = inst[i].sub_base + (uint32_t)q;
-        },
-        nc);
+    parallel_for(nchunk, [&](size_t c) {
+      for_chunk(c, [&](size_t j, size_t i, size_t q) { plan.direct[j] = inst[i].sub_base + (uint32_t)q; });
+    }, nc);
     return SP_OK;
   }
-  std::vector<double> pred(nc), inst_total(ni, 0.0);
-  std::vector<uint32_t> csub(nc);
-  std::vector<int16_t> room(nc);  // levels left below the root before the limit
-  parallel_for(ni, [&](size_t i) {
-    Instance &I = inst[i];
-    const size_t na = off[i + 1] - off[i];
-    if (!na) return;
-    double growth = 6.0;
-    if (I.prev_total > 0 && I.last_total > 0)
-      growth = std::min(30.0, std::max(2.0, (double)I.last_total / (double)I.prev_total));
-    double tot = 0;
-    for (size_t q = 0; q < na; ++q) {
-      const double p = (double)I.last_load[q] * growth;
-      pred[off[i] + q] = p;
-      csub[off[i] + q] = I.sub_base + (uint32_t)q;
-      room[off[i] + q] = (int16_t)(limits[i] - (int)I.tmpl->D);
-      tot += p;
-    }
-    inst_total[i] = tot;
-  }, nc);
+  // predicted load of each candidate: the previous round's load x the
+  // instance's growth per threshold step (whose round total is the
+  // instance's last total x growth), or, with the learned balancer, below
+  std::vector<double> growth(ni, 0.0);
   double total = 0;
-  for (double t : inst_total) total += t;
+  for (size_t i = 0; i < ni; ++i) {
+    const Instance &I = inst[i];
+    if (off[i + 1] == off[i]) continue;
+    double gr = 6.0;
+    if (I.prev_total > 0 && I.last_total > 0)
+      gr = std::min(30.0, std::max(2.0, (double)I.last_total / (double)I.prev_total));
+    growth[i] = gr;
+    total += (double)I.last_total * gr;
+  }
+  std::vector<double> lpred;  // learned balancer: per candidate
   if (learned && nc) {
     // The model predicts every active root: y(s) = log2(1 + nodes) of its
     // subtree at slack s = (limit - g - h) / 2 (clamped to the slacks it was
@@ -898,6 +902,7 @@ int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int3
                                   s->err);
     if (rc) return rc;
     s->stats.kernel_launches += 2 * (int)((q_sub.size() + 65535) / 65536);
+    lpred.resize(nc);
     total = 0;
     size_t at = 0;
     for (size_t i = 0; i < ni; ++i) {
@@ -914,7 +919,7 @@ int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int3
           p = std::exp2(yh) - 1.0;
           at += 1;
         }
-        pred[j] = p;
+        lpred[j] = p;
         total += p;
       }
     }
@@ -924,28 +929,36 @@ int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int3
   static const size_t pow3[12] = {1, 3, 9, 27, 81, 243, 729, 2187, 6561, 19683, 59049, 177147};
   auto bound = [&](int kk) { return kk ? 4 * pow3[kk - 1] : (size_t)0; };
   const int kcap = std::min(10, std::max(1, s->cfg.static_split_cap));
-  // exponent of pred relative to T (ceil(log2(pred/T)) for pred > T): the
-  // split depth and the bucket of the longest-first order (bucket 63 - e:
-  // larger predictions first)
+  // pass 1, per chunk: the exponent of pred relative to T (ceil(log2(pred/T))
+  // for pred > T) gives the split depth and the bucket of the longest-first
+  // order (bucket 63 - e: larger predictions first); histograms of the
+  // buckets (whole and split roots apart) and of the split depths
   std::vector<int8_t> k(nc, 0);
   std::vector<uint8_t> bucket(nc, 127);
-  const size_t nchunk = std::max<size_t>(1, std::min<size_t>(64, nc / 8192));
-  auto chunk_lo = [&](size_t c) { return nc * c / nchunk; };
-  std::vector<size_t> kh(nchunk * 11, 0);  // per chunk: roots per split depth
+  std::vector<uint32_t> hd(nchunk * 128, 0), hs(nchunk * 128, 0);
+  std::vector<size_t> kh(nchunk * 11, 0);
   parallel_for(nchunk, [&](size_t c) {
-    for (size_t j = chunk_lo(c); j < chunk_lo(c + 1); ++j) {
+    uint32_t *cd = &hd[c * 128], *cs = &hs[c * 128];
+    size_t *ck = &kh[c * 11];
+    for_chunk(c, [&](size_t j, size_t i, size_t q) {
+      const double pred = learned ? lpred[j] : (double)inst[i].last_load[q] * growth[i];
       int e = -64;
-      if (pred[j] > 0 && T > 0) {
-        std::frexp(pred[j] / T, &e);  // pred/T in [2^(e-1), 2^e)
+      if (pred > 0 && T > 0) {
+        std::frexp(pred / T, &e);  // pred/T in [2^(e-1), 2^e)
         e = std::max(-63, std::min(63, e));
       }
-      bucket[j] = (uint8_t)(63 - e);
-      if (T > 0 && pred[j] > T) {
-        k[j] = (int8_t)std::max(0, std::min(e, std::min(kcap, (int)room[j] - 1)));
-        ++kh[c * 11 + k[j]];
+      const uint8_t b = (uint8_t)(63 - e);
+      bucket[j] = b;
+      int kk = 0;
+      if (T > 0 && pred > T) {
+        const int room = limits[i] - (int)inst[i].tmpl->D;  // levels left below the root
+        kk = std::max(0, std::min(e, std::min(kcap, room - 1)));
       }
-    }
-  });
+      k[j] = (int8_t)kk;
+      ++ck[kk];
+      ++(kk > 0 ? cs : cd)[b];
+    });
+  }, nc);
   // piece budget: the deepest splits are cut first, i.e. every depth is
   // capped at the largest cap whose pieces fit
   size_t cnt_k[11] = {0};
@@ -958,16 +971,10 @@ int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int3
     for (int kk = 1; kk <= 10; ++kk) need += cnt_k[kk] * bound(std::min(kk, kmax));
     if (need <= budget) break;
   }
-  if (kmax < 10)
-    parallel_for(nchunk, [&](size_t c) {
-      for (size_t j = chunk_lo(c); j < chunk_lo(c + 1); ++j) k[j] = (int8_t)std::min((int)k[j], kmax);
-    });
-  // stable counting sort by bucket, split roots and whole roots separately:
-  // per-chunk histograms, then every chunk scatters into its own ranges
-  std::vector<uint32_t> hd(nchunk * 128, 0), hs(nchunk * 128, 0);
-  parallel_for(nchunk, [&](size_t c) {
-    for (size_t j = chunk_lo(c); j < chunk_lo(c + 1); ++j) ++(k[j] > 0 ? hs : hd)[c * 128 + bucket[j]];
-  });
+  if (kmax == 0)  // no split fits: every root goes whole
+    for (size_t x = 0; x < hd.size(); ++x) hd[x] += hs[x], hs[x] = 0;
+  // stable counting sort by bucket, split roots and whole roots apart:
+  // every chunk scatters into its own ranges (pass 2)
   size_t nd = 0, nsp = 0;
   for (int b = 0; b < 128; ++b)
     for (size_t c = 0; c < nchunk; ++c) {
@@ -980,25 +987,31 @@ int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int3
   plan.direct.resize(nd);
   plan.split.resize(nsp);
   parallel_for(nchunk, [&](size_t c) {
-    for (size_t j = chunk_lo(c); j < chunk_lo(c + 1); ++j) {
-      if (k[j] > 0) {
+    uint32_t *cd = &hd[c * 128], *cs = &hs[c * 128];
+    for_chunk(c, [&](size_t j, size_t i, size_t q) {
+      const int kk = std::min((int)k[j], kmax);
+      const uint32_t sub = inst[i].sub_base + (uint32_t)q;
+      if (kk > 0) {
         Task t{};
-        t.sub = csub[j];
+        t.sub = sub;
         t.mask = 0xF;
-        t.flags = (uint8_t)k[j];
-        plan.split[hs[c * 128 + bucket[j]]++] = t;
+        t.flags = (uint8_t)kk;
+        plan.split[cs[bucket[j]]++] = t;
       } else {
-        plan.direct[hd[c * 128 + bucket[j]]++] = csub[j];
+        plan.direct[cd[bucket[j]]++] = sub;
       }
-    }
-  });
-  size_t level[12] = {0};
-  for (const Task &t : plan.split) {
-    const int kk = t.flags;
-    plan.max_k = std::max(plan.max_k, kk);
-    for (int l = 1; l <= kk; ++l) level[l] += 4 * pow3[l - 1];
-    plan.emit_bound += bound(kk);
+    });
+  }, nc);
+  for (int kk = 1; kk <= 10; ++kk) {
+    const size_t cnt = cnt_k[kk];
+    if (!cnt || kmax == 0) continue;
+    const int ke = std::min(kk, kmax);
+    plan.max_k = std::max(plan.max_k, ke);
+    plan.emit_bound += cnt * bound(ke);
   }
+  size_t level[12] = {0};
+  for (int kk = 1; kk <= 10 && kmax > 0; ++kk)
+    for (int l = 1; l <= std::min(kk, kmax); ++l) level[l] += cnt_k[kk] * 4 * pow3[l - 1];
   for (int l = 1; l < 12; ++l) plan.level_bound = std::max(plan.level_bound, level[l]);
   return SP_OK;
 }
