@@ -26,7 +26,7 @@
 namespace sp {
 namespace {
 
-constexpr int kFrontThreads = 256;
+constexpr int kFrontThreads = 1024;
 constexpr int kFrontWarps = kFrontThreads / 32;
 
 template <int W>

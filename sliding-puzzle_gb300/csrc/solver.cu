@@ -664,6 +664,12 @@ int ensure_pool(sp_solver *s, size_t n_init) {
 struct RoundPlan {
   std::vector<uint32_t> direct;
   std::vector<Task> split;
+  // the static planner writes straight into the solver's pinned staging
+  // buffers (h_direct, h_split) instead; the vectors above stay empty
+  bool staged = false;
+  size_t staged_direct = 0, staged_split = 0;
+  size_t n_direct() const { return staged ? staged_direct : direct.size(); }
+  size_t n_split() const { return staged ? staged_split : split.size(); }
   size_t level_bound = 0;  // nodes one split level can hold
   size_t emit_bound = 0;   // pieces the split pre-pass can emit
   int max_k = 0;
@@ -689,36 +695,41 @@ void fold_ctl(sp_solver *s, const PoolCtl &ctl, int ri, float ms) {
 // control block, split counters, per-root counts and solutions come back.
 int launch_round(sp_solver *s, const RoundPlan &plan, size_t n_subs, size_t n_inst, float *ms,
                  bool multi = false) {
-  const uint32_t n_direct = (uint32_t)plan.direct.size();
-  int rc = ensure_pool(s, plan.direct.size() + plan.emit_bound);
+  const uint32_t n_direct = (uint32_t)plan.n_direct();
+  const size_t n_split = plan.n_split();
+  int rc = ensure_pool(s, n_direct + plan.emit_bound);
   if (rc) return rc;
   rc = ensure(s, &s->d_direct, &s->direct_cap, std::max<size_t>(n_direct, 1));
   if (rc) return rc;
   if (!s->d_cnt) SP_CUDA(s, cudaMalloc(&s->d_cnt, 4 * sizeof(uint32_t)));
   SP_CUDA(s, s->h_cnt.reserve(4));
   if (n_direct) {
-    SP_CUDA(s, s->h_direct.reserve(n_direct));
-    memcpy(s->h_direct.p, plan.direct.data(), n_direct * sizeof(uint32_t));
+    if (!plan.staged) {
+      SP_CUDA(s, s->h_direct.reserve(n_direct));
+      memcpy(s->h_direct.p, plan.direct.data(), n_direct * sizeof(uint32_t));
+    }
     SP_CUDA(s, cudaMemcpyAsync(s->d_direct, s->h_direct.p, n_direct * sizeof(uint32_t), cudaMemcpyHostToDevice,
                                s->st));
     s->stats.h2d_bytes += n_direct * sizeof(uint32_t);
   }
-  s->h_cnt.p[0] = (uint32_t)plan.split.size();
+  s->h_cnt.p[0] = (uint32_t)n_split;
   s->h_cnt.p[1] = s->h_cnt.p[2] = s->h_cnt.p[3] = 0;
   SP_CUDA(s, cudaMemcpyAsync(s->d_cnt, s->h_cnt.p, 4 * sizeof(uint32_t), cudaMemcpyHostToDevice, s->st));
-  if (!plan.split.empty()) {
-    const size_t lb = std::max(plan.level_bound, plan.split.size());
+  if (n_split) {
+    const size_t lb = std::max(plan.level_bound, n_split);
     rc = ensure(s, &s->d_split_a, &s->split_cap_a, lb);
     if (rc) return rc;
     rc = ensure(s, &s->d_split_b, &s->split_cap_b, lb);
     if (rc) return rc;
     rc = ensure(s, &s->d_emit, &s->emit_cap, std::max<size_t>(plan.emit_bound, 1));
     if (rc) return rc;
-    SP_CUDA(s, s->h_split.reserve(plan.split.size()));
-    memcpy(s->h_split.p, plan.split.data(), plan.split.size() * sizeof(Task));
-    SP_CUDA(s, cudaMemcpyAsync(s->d_split_a, s->h_split.p, plan.split.size() * sizeof(Task),
+    if (!plan.staged) {
+      SP_CUDA(s, s->h_split.reserve(n_split));
+      memcpy(s->h_split.p, plan.split.data(), n_split * sizeof(Task));
+    }
+    SP_CUDA(s, cudaMemcpyAsync(s->d_split_a, s->h_split.p, n_split * sizeof(Task),
                                cudaMemcpyHostToDevice, s->st));
-    s->stats.h2d_bytes += plan.split.size() * sizeof(Task);
+    s->stats.h2d_bytes += n_split * sizeof(Task);
   }
   SP_CUDA(s, cudaEventRecord(s->ev0, s->st));
   for (int l = 0; l < plan.max_k; ++l) {
@@ -984,8 +995,13 @@ int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int3
       nd += a;
       nsp += z;
     }
-  plan.direct.resize(nd);
-  plan.split.resize(nsp);
+  SP_CUDA(s, s->h_direct.reserve(std::max<size_t>(nd, 1)));
+  SP_CUDA(s, s->h_split.reserve(std::max<size_t>(nsp, 1)));
+  uint32_t *out_direct = s->h_direct.p;
+  Task *out_split = s->h_split.p;
+  plan.staged = true;
+  plan.staged_direct = nd;
+  plan.staged_split = nsp;
   parallel_for(nchunk, [&](size_t c) {
     uint32_t *cd = &hd[c * 128], *cs = &hs[c * 128];
     for_chunk(c, [&](size_t j, size_t i, size_t q) {
@@ -996,9 +1012,9 @@ int plan_round(sp_solver *s, std::vector<Instance> &inst, const std::vector<int3
         t.sub = sub;
         t.mask = 0xF;
         t.flags = (uint8_t)kk;
-        plan.split[cs[bucket[j]]++] = t;
+        out_split[cs[bucket[j]]++] = t;
       } else {
-        plan.direct[cd[bucket[j]]++] = sub;
+        out_direct[cd[bucket[j]]++] = sub;
       }
     });
   }, nc);
@@ -1397,13 +1413,13 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
     float ms = 0;
     const unsigned long long *sn = nullptr;
     const Solution *sols = nullptr;
-    if (!plan.direct.empty() || !plan.split.empty()) {
+    if (plan.n_direct() || plan.n_split()) {
       rc = launch_round(s, plan, n_subs, inst.size(), &ms);
       if (rc) return rc;
       const PoolCtl &ctl = *s->h_ctl.p;
       fold_ctl(s, ctl, ri, ms);
-      s->stats.tasks_initial += plan.direct.size() + s->last_emitted;
-      s->stats.round_tasks[ri] = (int32_t)(plan.direct.size() + s->last_emitted);
+      s->stats.tasks_initial += plan.n_direct() + s->last_emitted;
+      s->stats.round_tasks[ri] = (int32_t)(plan.n_direct() + s->last_emitted);
       if (ctl.error) {
         char buf[160];
         snprintf(buf, sizeof buf, "device error %d (info %u) in round %d", ctl.error, ctl.err_info[0], round);
