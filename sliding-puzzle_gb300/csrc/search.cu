@@ -160,6 +160,45 @@ __device__ __forceinline__ uint32_t set_byte(uint32_t v, int p, uint32_t x) {
 // lanes of a warp with the same instance i; `hist` is the warp's 32 words of
 // shared memory.  Kept out of line: it is cold, and inlined its registers
 // would crowd the search loop.
+// Iteration r of instance i, published beside the one before it (warp
+// advance below): its limit and solution record (those of r - 2, whose goal
+// flag is clear), loads zeroed, its na roots (in maxf order, unsplit) at
+// pool indices t0 ... t0 + na - 1, already reserved.  Kept out of line so
+// that the search loop's registers do not pay for it.
+__device__ __noinline__ void publish_second(const RoundParams &P, uint32_t i, int r, int L, uint32_t base,
+                                            uint32_t ns, uint32_t t0, uint32_t na) {
+  const int lane = threadIdx.x & 31;
+  PoolCtl *ctl = P.ctl;
+  if (lane == 0) {
+    const_cast<int32_t *>(P.inst_limit)[2 * i + (r & 1)] = L;
+    P.inst_pair[i] = 1u;
+  }
+  unsigned long long *lz = P.sub_loads + (size_t)(r & 1) * P.n_subs + base;
+  for (uint32_t q = lane; q < ns; q += 32) lz[q] = 0;
+  __threadfence();
+  __syncwarp();
+  const uint32_t mask = P.cap - 1u;
+  for (uint32_t q = lane; q < na; q += 32) {
+    const uint32_t t = t0 + q;
+    bool free_slot = false;
+    for (int spin = 0; spin < (1 << 14) && !free_slot; ++spin) {
+      free_slot = ld_acquire(&P.seq[t & mask]) == t;
+      if (!free_slot) __nanosleep(64);
+    }
+    if (!free_slot) {
+      if (atomicCAS(&ctl->error, 0, SP_ERR_CAPACITY) == 0) ctl->err_info[0] = t;
+      continue;
+    }
+    Task *D = &P.tasks[t & mask];
+    D->sub = base + q;
+    D->plen = 0;
+    D->mask = 0xF;
+    D->flags = (uint8_t)((r & 1) << 6);
+    st_release(&P.seq[t & mask], t + 1u);
+  }
+  __syncwarp();
+}
+
 __device__ __noinline__ void warp_advance(const RoundParams &P, uint32_t i, uint32_t *hist) {
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
@@ -174,13 +213,36 @@ __device__ __noinline__ void warp_advance(const RoundParams &P, uint32_t i, uint
     }
     return lo ? P.inter_cum[off + lo - 1] : 0ull;
   };
+  // per instance, two limits and two solution records, by iteration parity
   int r = ld_volatile(&P.inst_iter[i]);
-  int L = ld_volatile(&P.inst_limit[i]);
+  int L = ld_volatile(&P.inst_limit[2 * i + (r & 1)]);
   if (lane == 0) atomicAdd(&P.iter_nodes[(size_t)i * kMaxIters + r], interior(L));
+  if (ld_volatile(&P.inst_pair[i])) {
+    // iterations r and r + 1 ran together and have both finished: r's goal
+    // decides first (r + 1's counts are then never read)
+    int stop = 0;
+    if (lane == 0) stop = (ld_volatile(&P.sol[2 * i + (r & 1)].flag) != 0u || P.goal_maxf[i] <= L) ? 1 : 0;
+    stop = __shfl_sync(FULL, stop, 0);
+    if (stop || r + 1 >= kMaxIters) {
+      if (lane == 0) {
+        P.inst_final[i] = r;
+        P.inst_fin_ns[i] = globaltimer();
+        if (!stop) P.inst_status[i] = SP_ERR_LIMIT;
+      }
+      return;
+    }
+    ++r;
+    L += 2;
+    if (lane == 0) {
+      P.inst_iter[i] = r;
+      P.inst_pair[i] = 0u;
+      atomicAdd(&P.iter_nodes[(size_t)i * kMaxIters + r], interior(L));
+    }
+  }
   for (;;) {
     // every task of iteration r has finished: the goal flag is final
     int stop = 0;
-    if (lane == 0) stop = (ld_volatile(&P.sol[i].flag) != 0u || P.goal_maxf[i] <= L) ? 1 : 0;
+    if (lane == 0) stop = (ld_volatile(&P.sol[2 * i + (r & 1)].flag) != 0u || P.goal_maxf[i] <= L) ? 1 : 0;
     stop = __shfl_sync(FULL, stop, 0);
     if (stop || r + 1 >= kMaxIters) {
       if (lane == 0) {
@@ -202,7 +264,7 @@ __device__ __noinline__ void warp_advance(const RoundParams &P, uint32_t i, uint
     const uint32_t na = lo;
     if (lane == 0) {
       P.inst_iter[i] = r;
-      const_cast<int32_t *>(P.inst_limit)[i] = L;
+      const_cast<int32_t *>(P.inst_limit)[2 * i + (r & 1)] = L;
       if (!na) atomicAdd(&P.iter_nodes[(size_t)i * kMaxIters + r], interior(L));
     }
     if (!na) continue;
@@ -265,12 +327,25 @@ __device__ __noinline__ void warp_advance(const RoundParams &P, uint32_t i, uint
       if (lane + o < 32) suf += v;
     }
     hist[lane] = suf - c;  // first position of bucket `lane`
-    // the whole iteration is outstanding before its first task is visible
+    // iteration r + 1 goes out with r when it is predicted small: the two
+    // run together and the instance advances once both have finished, so a
+    // chain of small iterations is not paced by one iteration at a time
+    uint32_t na2 = 0;
+    if (P.pair_nodes && r + 2 < kMaxIters && (double)tot * grow * grow < (double)P.pair_nodes) {
+      uint32_t lo2 = na, hi2 = ns;  // active roots of r + 1: prefix with maxf <= L + 2
+      while (lo2 < hi2) {
+        const uint32_t mid = (lo2 + hi2) >> 1;
+        if (P.sub_maxf[base + mid] <= L + 2) lo2 = mid + 1;
+        else hi2 = mid;
+      }
+      na2 = lo2;
+    }
+    // the whole iteration (pair) is outstanding before its first task is visible
     uint32_t t0 = 0;
     if (lane == 0) {
-      atomicAdd(&P.inst_out[i], na);
-      atomicAdd(&ctl->outstanding, na);
-      t0 = atomicAdd(&ctl->tail, na);
+      atomicAdd(&P.inst_out[i], na + na2);
+      atomicAdd(&ctl->outstanding, na + na2);
+      t0 = atomicAdd(&ctl->tail, na + na2);
       __threadfence();
     }
     t0 = __shfl_sync(FULL, t0, 0);
@@ -302,10 +377,11 @@ __device__ __noinline__ void warp_advance(const RoundParams &P, uint32_t i, uint
       D->sub = base + q;
       D->plen = 0;
       D->mask = 0xF;
-      D->flags = (uint8_t)kk;
+      D->flags = (uint8_t)(kk | ((r & 1) << 6));  // bit 6: the iteration's parity
       st_release(&P.seq[t & mask], t + 1u);
     }
     __syncwarp();
+    if (na2) publish_second(P, i, r + 1, L + 2, base, ns, t0 + na, na2);
     return;
   }
 }
@@ -392,7 +468,9 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
   ir.clear();
   iff.clear();
   unsigned long long c_tries = 0, c_notfree = 0, c_nowait = 0, c_done = 0, c_found = 0;  // donation counters
-  uint32_t cur_inst = 0;  // the task's instance
+  // the task's instance; multi-iteration mode: bit 31 = the parity of the
+  // task's iteration (kept in the same register: the search loop has none to spare)
+  uint32_t cur_inst = 0;
   int splitk = 0;         // split task: hand every node at this relative depth to the pool
   bool emit_pending = false;
   // Rare per-lane events, flags in a register and their data in shared memory:
@@ -485,18 +563,21 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
     state = 0;
     if (MULTI) {
       if (cnt) {
-        // the instance stays in the task's iteration while the task is outstanding
-        const int cur_iter = ld_volatile(&P.inst_iter[cur_inst]);
-        atomicAdd(&P.iter_nodes[(size_t)cur_inst * kMaxIters + cur_iter], cnt);
-        atomicAdd(&P.sub_loads[(size_t)(cur_iter & 1) * P.n_subs + sub], cnt);
+        // the instance stays in its current iteration while the task is
+        // outstanding; the task's own is that one or, in a pair, the next
+        const uint32_t ci = cur_inst & 0x7FFFFFFFu, tp = cur_inst >> 31;
+        const int cur_iter = ld_volatile(&P.inst_iter[ci]);
+        const int task_iter = cur_iter + (((uint32_t)cur_iter & 1u) != tp ? 1 : 0);
+        atomicAdd(&P.iter_nodes[(size_t)ci * kMaxIters + task_iter], cnt);
+        atomicAdd(&P.sub_loads[(size_t)tp * P.n_subs + sub], cnt);
       }
       __threadfence();
       // the last task of the iteration: the warp advances the instance at the
       // top of its next loop, and only then does this task leave
       // `outstanding`, so that never reads 0 while work is still to come
-      if (atomicSub(&P.inst_out[cur_inst], 1u) == 1u) {
+      if (atomicSub(&P.inst_out[cur_inst & 0x7FFFFFFFu], 1u) == 1u) {
         events |= kAdvance;
-        s_cold[0][tid] = cur_inst;
+        s_cold[0][tid] = cur_inst & 0x7FFFFFFFu;
         return;
       }
     } else if (cnt) {
@@ -514,7 +595,8 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
     const uint32_t hdr = __ldcg((const uint32_t *)T + 1);
     plen = (int)(hdr & 0xFFFFu);
     mask0 = (hdr >> 16) & 0xFu;
-    splitk = (int)(hdr >> 24);
+    splitk = MULTI ? (int)((hdr >> 24) & 0x3Fu) : (int)(hdr >> 24);
+    cur_inst = MULTI ? (hdr << 1) & 0x80000000u : 0u;  // the parity bit until start_task adds the instance
     for (int wi = 0; wi < kPathWords; ++wi) s_prefix[wi][tid] = __ldcg(&T->path[wi]);
     st_release(&P.seq[s], slot + P.cap);  // the copy above completes before the slot is reused
   };
@@ -535,10 +617,11 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
     g = tb[26 - 16];
     pre = tb[27 - 16] == kNoPre ? -1 : (int)tb[27 - 16];
     uint32_t inst = *(const uint32_t *)(tb + 12);
-    cur_inst = inst;
     if (MULTI) {
-      limit = ld_volatile(&P.inst_limit[inst]);
+      limit = ld_volatile(&P.inst_limit[2 * inst + (cur_inst >> 31)]);
+      cur_inst |= inst;
     } else {
+      cur_inst = inst;
       limit = P.inst_limit[inst];
     }
     for (int i = 0; i < plen; ++i) {
@@ -566,7 +649,8 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
     return g + h <= limit;
   };
   auto record_goal = [&]() {
-    Solution *S = &P.sol[P.subs[sub].inst];
+    const uint32_t si = P.subs[sub].inst;
+    Solution *S = &P.sol[MULTI ? 2 * si + (cur_inst >> 31) : si];
     atomicMax(&S->best, 0xFFFFFFFFu - (uint32_t)g);  // shortest goal depth over all lanes
     if (atomicCAS(&S->flag, 0u, 1u) == 0u) {
       int len = plen + k;
@@ -825,7 +909,7 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
         bool emitted = false;
         if (!(events & kDebt) && (int32_t)(tl - hd) <= (int32_t)(P.cap >> 1)) {
           atomicAdd(&ctl->outstanding, 1u);
-          if (MULTI) atomicAdd(&P.inst_out[cur_inst], 1u);  // the lane's own task keeps it >= 1
+          if (MULTI) atomicAdd(&P.inst_out[cur_inst & 0x7FFFFFFFu], 1u);  // the lane's own task keeps it >= 1
           const uint32_t t = atomicAdd(&ctl->tail, 1u);
           if (slot_free(t, 4096)) {
             const int len = plen + k;
@@ -833,7 +917,7 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
             D->sub = sub;
             D->plen = (uint16_t)len;
             D->mask = 0xF;
-            D->flags = (uint8_t)(splitk - 1);
+            D->flags = (uint8_t)((splitk - 1) | (MULTI ? (cur_inst >> 31) << 6 : 0u));
             for (int wi = 0; wi < kPathWords; ++wi) D->path[wi] = path_word(wi, len);
             st_release(&P.seq[t & (P.cap - 1u)], t + 1u);
             emitted = true;
@@ -881,7 +965,7 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
         // branch and owe the index a null task
         const uint32_t mask = P.cap - 1u;
         ++c_tries;
-        if (MULTI) atomicAdd(&P.inst_out[cur_inst], 1u);  // the donor's own task keeps it >= 1
+        if (MULTI) atomicAdd(&P.inst_out[cur_inst & 0x7FFFFFFFu], 1u);  // the donor's own task keeps it >= 1
         const uint32_t t = tbase + (uint32_t)__popc(donors & ((1u << lane) - 1u));
         const bool ok = slot_free(t, 4096);
         if (!ok) {
@@ -896,7 +980,7 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
           D->sub = sub;
           D->plen = (uint16_t)nlen;
           D->mask = (uint8_t)dmask;
-          D->flags = 0;
+          D->flags = (uint8_t)(MULTI ? (cur_inst >> 31) << 6 : 0u);
           for (int wi = 0; wi < kPathWords; ++wi) D->path[wi] = path_word(wi, nlen);
           st_release(&P.seq[t & mask], t + 1u);
           atomicAdd(&ctl->donated, 1ull);
@@ -934,7 +1018,8 @@ __global__ void __launch_bounds__(BLOCK, SP_SEARCH_THREADS_PER_SM / BLOCK) searc
 // of split roots (count on the device) come first, then the host's direct
 // tasks, which the host orders by decreasing predicted size.
 __global__ void pool_init_kernel(Task *tasks, const Task *emit, const uint32_t *n_emit, const uint32_t *direct,
-                                 uint32_t n_direct, uint32_t *seq, uint32_t cap, PoolCtl *ctl) {
+                                 uint32_t n_direct, uint32_t *seq, uint32_t cap, PoolCtl *ctl, const SubRoot *subs,
+                                 const int32_t *inst_iter) {
   const uint32_t ne = n_emit ? *n_emit : 0u;
   const uint32_t n = min(ne + n_direct, cap);
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < cap; i += gridDim.x * blockDim.x) {
@@ -945,6 +1030,7 @@ __global__ void pool_init_kernel(Task *tasks, const Task *emit, const uint32_t *
         Task t{};
         t.sub = direct[i - ne];
         t.mask = 0xF;
+        if (inst_iter) t.flags = (uint8_t)((inst_iter[subs[t.sub].inst] & 1) << 6);
         tasks[i] = t;
       }
       seq[i] = i + 1u;
@@ -1095,9 +1181,10 @@ cudaError_t launch_search_multi(int w, bool pdb, int block, int blocks_per_sm, i
 }
 
 cudaError_t launch_pool_init(Task *tasks, const Task *emit, const uint32_t *n_emit, const uint32_t *direct,
-                             uint32_t n_direct, uint32_t *seq, uint32_t cap, PoolCtl *ctl, cudaStream_t st) {
+                             uint32_t n_direct, uint32_t *seq, uint32_t cap, PoolCtl *ctl, const SubRoot *subs,
+                             const int32_t *inst_iter, cudaStream_t st) {
   const uint32_t blocks = std::min<uint32_t>((cap + 255) / 256, 152u * 32u);
-  pool_init_kernel<<<blocks, 256, 0, st>>>(tasks, emit, n_emit, direct, n_direct, seq, cap, ctl);
+  pool_init_kernel<<<blocks, 256, 0, st>>>(tasks, emit, n_emit, direct, n_direct, seq, cap, ctl, subs, inst_iter);
   note_launch();
   return cudaGetLastError();
 }

@@ -60,6 +60,20 @@
 #define SP_SPLIT_PIECES_PER_LANE 1.0
 #endif
 
+// Device loop: an instance's next two iterations run together (the instance
+// advances once both are done) when the second is predicted below this many
+// generated nodes -- in the hybrid loop, for batches of at most one instance
+// per SP_PAIR_LANES resident lanes, where a chain of small iterations per
+// instance leaves the GPU underused (measured: yama24_50_hard_new -5 %,
+// the 15-puzzle batches of 100 -1 to -2 %; a 4096-instance batch, which
+// fills the GPU anyway, +1.8 %, and the pure device loop much slower).
+#ifndef SP_PAIR_NODES
+#define SP_PAIR_NODES 300000
+#endif
+#ifndef SP_PAIR_LANES
+#define SP_PAIR_LANES 256
+#endif
+
 // Shortest interval between two reads of the pool's control words by one
 // block (ns); the block shares what it read.
 #ifndef SP_POLL_NS
@@ -158,15 +172,15 @@ struct Pinned {
 // Device tables of the multi-iteration mode (grow-only).
 struct MultiBufs {
   int32_t *iter = nullptr, *fin = nullptr, *status = nullptr, *goal = nullptr, *ifv = nullptr;
-  uint32_t *out = nullptr, *base = nullptr, *nsub = nullptr, *ioff = nullptr, *ilen = nullptr;
+  uint32_t *out = nullptr, *base = nullptr, *nsub = nullptr, *ioff = nullptr, *ilen = nullptr, *pair = nullptr;
   unsigned long long *icum = nullptr, *iter_nodes = nullptr, *loads = nullptr, *fin_ns = nullptr, *t0_ns = nullptr;
   uint8_t *growth = nullptr;  // learned balancer: [n_subs][kGrowthSlacks] growth codes
   size_t cap_iter = 0, cap_fin = 0, cap_status = 0, cap_goal = 0, cap_ifv = 0, cap_out = 0,
-         cap_base = 0, cap_nsub = 0, cap_ioff = 0, cap_ilen = 0, cap_icum = 0, cap_iter_nodes = 0, cap_loads = 0,
+         cap_base = 0, cap_nsub = 0, cap_ioff = 0, cap_ilen = 0, cap_icum = 0, cap_iter_nodes = 0, cap_loads = 0, cap_pair = 0,
          cap_fin_ns = 0, cap_t0_ns = 0, cap_growth = 0;
   bool use_growth = false;  // the current launch has growth codes
   void release() {
-    void *ptrs[] = {iter, fin,  status, goal, ifv,        out,   base,   nsub,
+    void *ptrs[] = {iter, fin,  status, goal, ifv,        out,   base,   nsub, pair,
                     ioff, ilen, icum,   iter_nodes, loads, fin_ns, t0_ns, growth};
     for (void *p : ptrs) cudaFree(p);
   }
@@ -755,7 +769,8 @@ int launch_round(sp_solver *s, const RoundPlan &plan, size_t n_subs, size_t n_in
     s->stats.kernel_launches += 1;
   }
   SP_CUDA(s, launch_pool_init(s->d_tasks, s->d_emit, plan.max_k ? s->d_cnt + 2 : nullptr, s->d_direct, n_direct,
-                              s->d_seq, s->cap, s->d_ctl, s->st));
+                              s->d_seq, s->cap, s->d_ctl, multi ? s->d_subs : nullptr, multi ? s->mb.iter : nullptr,
+                              s->st));
   RoundParams P{};
   P.subs = s->d_subs;
   P.tasks = s->d_tasks;
@@ -792,6 +807,8 @@ int launch_round(sp_solver *s, const RoundPlan &plan, size_t n_subs, size_t n_in
     P.inter_f = m.ifv;
     P.inter_cum = m.icum;
     P.goal_maxf = m.goal;
+    P.inst_pair = m.pair;
+    P.pair_nodes = (s->cfg.handback_nodes > 0 && n_inst * SP_PAIR_LANES <= (size_t)lanes) ? SP_PAIR_NODES : 0;
     P.iter_nodes = m.iter_nodes;
     P.sub_loads = m.loads;
     P.inst_fin_ns = m.fin_ns;
@@ -815,11 +832,13 @@ int launch_round(sp_solver *s, const RoundPlan &plan, size_t n_subs, size_t n_in
   if (n_subs && !multi)
     SP_CUDA(s, cudaMemcpyAsync(s->h_sub_nodes.p, s->d_sub_nodes, n_subs * sizeof(unsigned long long),
                                cudaMemcpyDeviceToHost, s->st));
+  const size_t n_sol = multi ? 2 * n_inst : n_inst;  // multi: one record per instance and iteration parity
+  SP_CUDA(s, s->h_sols.reserve(std::max<size_t>(n_sol, 1)));
   if (n_inst)
-    SP_CUDA(s, cudaMemcpyAsync(s->h_sols.p, s->d_sol, n_inst * sizeof(Solution), cudaMemcpyDeviceToHost, s->st));
+    SP_CUDA(s, cudaMemcpyAsync(s->h_sols.p, s->d_sol, n_sol * sizeof(Solution), cudaMemcpyDeviceToHost, s->st));
   SP_CUDA(s, cudaStreamSynchronize(s->st));
   SP_CUDA(s, cudaEventElapsedTime(ms, s->ev0, s->ev1));
-  s->stats.d2h_bytes += sizeof(PoolCtl) + 16 + n_subs * 8 + n_inst * sizeof(Solution);
+  s->stats.d2h_bytes += sizeof(PoolCtl) + 16 + n_subs * 8 + n_sol * sizeof(Solution);
   s->stats.kernel_launches += 2;
   s->last_lanes = grid * block;
   s->last_emitted = s->h_cnt.p[2];
@@ -1083,7 +1102,9 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
                 std::chrono::steady_clock::time_point t_start) {
   const size_t ni = inst.size();
   const int w = s->w, n = s->n;
-  std::vector<int32_t> h_iter(ni, 0), h_limit(ni, 0), h_final(ni, -1), h_goal(ni, 0x7FFFFFFF);
+  // limits: two per instance, by iteration parity (the device loop may run an
+  // instance's next iteration beside the current one)
+  std::vector<int32_t> h_iter(ni, 0), h_limit(2 * ni, 0), h_final(ni, -1), h_goal(ni, 0x7FFFFFFF);
   std::vector<uint32_t> h_out(ni, 0), h_base(ni, 0), h_nsub(ni, 0), h_ioff(ni, 0), h_ilen(ni, 0);
   std::vector<int32_t> h_if;
   std::vector<unsigned long long> h_icum;
@@ -1108,7 +1129,7 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
         for (size_t q = 0; q < na; ++q) direct.push_back(I.sub_base + (uint32_t)q);
         h_out[i] = (uint32_t)na;
         h_iter[i] = I.iter;
-        h_limit[i] = L;
+        h_limit[2 * i + (I.iter & 1)] = L;
         break;
       }
       sp_result *R = I.out;
@@ -1147,7 +1168,8 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
       (rc = ensure(s, &m.ifv, &m.cap_ifv, h_if.size())) || (rc = ensure(s, &m.icum, &m.cap_icum, h_icum.size())) ||
       (rc = ensure(s, &m.iter_nodes, &m.cap_iter_nodes, ni * kMaxIters)) ||
       (rc = ensure(s, &m.loads, &m.cap_loads, 2 * std::max<size_t>(n_subs, 1))) ||
-      (rc = ensure(s, &m.fin_ns, &m.cap_fin_ns, ni)) || (rc = ensure(s, &m.t0_ns, &m.cap_t0_ns, 1)))
+      (rc = ensure(s, &m.fin_ns, &m.cap_fin_ns, ni)) || (rc = ensure(s, &m.t0_ns, &m.cap_t0_ns, 1)) ||
+      (rc = ensure(s, &m.pair, &m.cap_pair, ni)))
     return rc;
   // uploads through one pinned staging buffer (asynchronous copies)
   auto bytes16 = [](const auto &v) { return (v.size() * sizeof(v[0]) + 15) & ~(size_t)15; };
@@ -1177,7 +1199,8 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
   SP_CUDA(s, up(m.icum, h_icum));
   SP_CUDA(s, cudaMemsetAsync(m.iter_nodes, 0, ni * kMaxIters * sizeof(unsigned long long), s->st));
   SP_CUDA(s, cudaMemsetAsync(m.loads, 0, 2 * std::max<size_t>(n_subs, 1) * sizeof(unsigned long long), s->st));
-  SP_CUDA(s, cudaMemsetAsync(s->d_sol, 0, ni * sizeof(Solution), s->st));
+  SP_CUDA(s, cudaMemsetAsync(s->d_sol, 0, 2 * ni * sizeof(Solution), s->st));
+  SP_CUDA(s, cudaMemsetAsync(m.pair, 0, ni * sizeof(uint32_t), s->st));
   SP_CUDA(s, cudaMemsetAsync(m.fin_ns, 0, ni * sizeof(unsigned long long), s->st));
   SP_CUDA(s, cudaMemsetAsync(m.t0_ns, 0xFF, sizeof(unsigned long long), s->st));
   // learned balancer: every root's predicted growth per threshold step at
@@ -1316,7 +1339,7 @@ int solve_multi(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &inst,
     } else {
       const int L = I.h0 + 2 * fin[i];
       const int hg = tree_goal(I, L);
-      set_path(w, I, tiles + i * (size_t)n, hg, hg < 0 ? &sols[i] : nullptr, s->fb.h_leaf_node.p);
+      set_path(w, I, tiles + i * (size_t)n, hg, hg < 0 ? &sols[2 * i + (fin[i] & 1)] : nullptr, s->fb.h_leaf_node.p);
     }
     I.done = true;
   }
@@ -1372,8 +1395,9 @@ int solve_impl(sp_solver *s, const uint8_t *tiles, int nin, sp_result *res) {
     s->d_limit = nullptr;
     s->d_sol = nullptr;
     const size_t c = std::max<size_t>(inst.size(), 64);
-    SP_CUDA(s, cudaMalloc(&s->d_limit, c * sizeof(int32_t)));
-    SP_CUDA(s, cudaMalloc(&s->d_sol, c * sizeof(Solution)));
+    // two entries per instance: the device loop keeps one per iteration parity
+    SP_CUDA(s, cudaMalloc(&s->d_limit, 2 * c * sizeof(int32_t)));
+    SP_CUDA(s, cudaMalloc(&s->d_sol, 2 * c * sizeof(Solution)));
     s->inst_cap = c;
   }
   SP_CUDA(s, s->h_limits.reserve(inst.size()));
@@ -1780,7 +1804,8 @@ int sp_selftest_stall(sp_solver *s, int timeout_ms, int32_t *device_status) {
   }
   // an empty pool, then one task counted as queued at index 0 that no
   // producer ever publishes: every lane that claims it waits for it
-  SP_CUDA(s, launch_pool_init(s->d_tasks, nullptr, nullptr, nullptr, 0, s->d_seq, s->cap, s->d_ctl, s->st));
+  SP_CUDA(s, launch_pool_init(s->d_tasks, nullptr, nullptr, nullptr, 0, s->d_seq, s->cap, s->d_ctl, nullptr, nullptr,
+                              s->st));
   SP_CUDA(s, s->h_cnt.reserve(4));
   s->h_cnt.p[0] = 1;
   SP_CUDA(s, cudaMemcpyAsync(&s->d_ctl->tail, s->h_cnt.p, sizeof(uint32_t), cudaMemcpyHostToDevice, s->st));

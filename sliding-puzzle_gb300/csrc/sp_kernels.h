@@ -31,7 +31,9 @@ struct RoundParams {
   unsigned long long timeout_ns;
   unsigned long long poll_ns;  // min interval of a block's global pool poll
   // multi-iteration mode: every instance runs its own threshold loop on the
-  // device (inst_limit is then written by the kernel as well)
+  // device; inst_limit and sol then hold two entries per instance, indexed
+  // 2 * instance + (iteration & 1), and inst_limit is written by the kernel
+  // as well
   int32_t *inst_iter;                 // current iteration
   uint32_t *inst_out;                 // tasks of the current iteration not finished
   int32_t *inst_final;                // iteration that ended the search, -1 while running
@@ -43,6 +45,9 @@ struct RoundParams {
   const int32_t *inter_f;             //   of root-set interior nodes, sorted by f
   const unsigned long long *inter_cum;
   const int32_t *goal_maxf;           // smallest maxf of a root-set goal node (INT32_MAX: none)
+  uint32_t *inst_pair;                // 1: iterations inst_iter and inst_iter + 1 run together
+  unsigned long long pair_nodes;      // run the next two iterations together when the second is
+                                      //   predicted below this many nodes (0: one at a time)
   unsigned long long *iter_nodes;     // [instance][kMaxIters] generated nodes
   unsigned long long *sub_loads;      // [2][n_subs] per-root loads of the last two iterations
   unsigned long long *inst_fin_ns;    // %globaltimer when the instance's answer became final
@@ -65,8 +70,11 @@ cudaError_t launch_search_multi(int w, bool pdb, int block, int blocks_per_sm, i
                                 const RoundParams &P, cudaStream_t st, int *grid_out);
 // Publish the round's tasks (split pieces first, then the direct tasks) and
 // reset the pool control block.
+// Multi-iteration mode passes subs and inst_iter: each direct task then
+// carries its instance's iteration parity.
 cudaError_t launch_pool_init(Task *tasks, const Task *emit, const uint32_t *n_emit, const uint32_t *direct,
-                             uint32_t n_direct, uint32_t *seq, uint32_t cap, PoolCtl *ctl, cudaStream_t st);
+                             uint32_t n_direct, uint32_t *seq, uint32_t cap, PoolCtl *ctl, const SubRoot *subs,
+                             const int32_t *inst_iter, cudaStream_t st);
 
 // Split pre-pass: one breadth-first level over `in` (count *n_in).
 struct SplitArgs {
