@@ -322,7 +322,7 @@ AUTOTUNE_SPACE = (
     ("threads_per_block", (256, 128)),
     ("steps_per_poll", (32, 16, 64)),
     ("persistent", (1, 0)),
-    ("handback_nodes", (600000, 0, 100000, 3000000)),
+    ("handback_nodes", (600000, 300000, 1200000, 0, 3000000)),
     ("donate_reserve", (0, -1, 30000)),
     ("donate_min_slack", (6, 4, 8, 10)),
     ("frontier_target", (2048, 1024, 4096, 8192, 16384)),
