@@ -109,7 +109,7 @@ typedef struct {
 #define SP_MAX_ROUNDS 96
 
 typedef struct {
-  double frontier_ms;        /* host root-set construction */
+  double frontier_ms;        /* root-set construction (host templates + one device launch) */
   double kernel_ms;          /* device time of the round kernels (events) */
   double wall_ms;            /* whole call */
   int32_t rounds;
