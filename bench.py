@@ -570,7 +570,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--instances", type=int, default=100)
-    ap.add_argument("--frontier", type=int, default=2048)
+    ap.add_argument("--frontier", type=int, default=3072)
     ap.add_argument("--lb", default="static")
     ap.add_argument("--persistent", type=int, default=None, choices=[0, 1],
                     help="threshold loop on the device (default: the library's, 1)")

@@ -71,7 +71,8 @@ typedef enum {
 } sp_lb_mode;
 
 typedef struct {
-  int32_t frontier_target;   /* subproblems per instance (reference BLOCK_NUM 2048);
+  int32_t frontier_target;   /* subproblems per instance (default 3072; the
+                                reference's BLOCK_NUM is 2048);
                                 a batch is capped near 8 per resident GPU lane
                                 (at least 32 per instance) */
   int32_t threads_per_block; /* 128 or 256 */

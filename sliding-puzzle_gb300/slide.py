@@ -325,7 +325,7 @@ AUTOTUNE_SPACE = (
     ("handback_nodes", (600000, 300000, 1200000, 0, 3000000)),
     ("donate_reserve", (0, -1, 30000)),
     ("donate_min_slack", (6, 4, 8, 10)),
-    ("frontier_target", (2048, 1024, 4096, 8192, 16384)),
+    ("frontier_target", (3072, 2048, 1024, 4096, 8192, 16384)),
 )
 
 

@@ -54,7 +54,7 @@ def test_status_strings_and_config_default():
         s = lib.sp_status_string(st).decode()
         assert s and s != "unknown status", st
     cfg = slide.default_config()
-    assert cfg.frontier_target == 2048 and cfg.threads_per_block in (128, 256)
+    assert cfg.frontier_target == 3072 and cfg.threads_per_block in (128, 256)
     assert lib.sp_pdb_table_size(4) == 16 * 15 * 14 * 13 * 12
     assert lib.sp_pdb_table_size(5) == 25 * 24 * 23 * 22 * 21 * 20
     assert lib.sp_pdb_num_tables(4) == 3 and lib.sp_pdb_num_tables(5) == 2
