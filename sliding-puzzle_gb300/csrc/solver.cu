@@ -601,21 +601,25 @@ int build_root_sets(sp_solver *s, const uint8_t *tiles, std::vector<Instance> &i
     SP_CUDA(s, cudaMemcpyAsync(fb.h_leaf_h.p, fb.leaf_h, n_subs, cudaMemcpyDeviceToHost, s->st));
     s->stats.d2h_bytes += n_subs;
   }
-  for (size_t k = 0; k < nl; ++k) {
+  // per instance only the buckets up to the last one in use (all leaves
+  // counted, no interior children or goals above it)
+  parallel_for(nl, [&](size_t k) {
     Instance &I = inst[live[k]];
     const FrontInst &O = fb.h_out.p[k];
+    int top = kFrontBuckets - 1;
+    while (top > 0 && O.leaf_cum[top - 1] == I.n_leaves && !O.child[top] && O.goal[top] == 0xFFFFFFFFu) --top;
     I.h0 = O.h0;
-    I.leaf_cum.assign(O.leaf_cum, O.leaf_cum + kFrontBuckets);
-    I.goal_key.assign(O.goal, O.goal + kFrontBuckets);
+    I.leaf_cum.assign(O.leaf_cum, O.leaf_cum + top + 1);
+    I.goal_key.assign(O.goal, O.goal + top + 1);
     I.interior.clear();
     uint64_t cum = 0;
-    for (uint32_t b = 0; b < (uint32_t)kFrontBuckets; ++b) {
+    for (int b = 0; b <= top; ++b) {
       if (!O.child[b]) continue;
       cum += O.child[b];
       I.interior.push_back({I.h0 + (int32_t)b, cum});
     }
     I.last_load.assign(I.n_leaves, 0);
-  }
+  }, nl * kFrontBuckets);
   return SP_OK;
 }
 
@@ -628,7 +632,7 @@ uint64_t interior_nodes(const Instance &I, int L) {
 
 size_t active_leaves(const Instance &I, int L) {
   if (L < I.h0) return 0;
-  return L - I.h0 >= kFrontBuckets ? I.n_leaves : I.leaf_cum[(size_t)(L - I.h0)];
+  return (size_t)(L - I.h0) >= I.leaf_cum.size() ? I.n_leaves : I.leaf_cum[(size_t)(L - I.h0)];
 }
 
 bool replay_ok(int w, const uint8_t *tiles, const uint8_t *moves, int len) {
@@ -1083,14 +1087,14 @@ void set_path(int w, Instance &I, const uint8_t *tiles, int host_goal, const Sol
 // within L, or -1.
 int tree_goal(const Instance &I, int L) {
   uint32_t best = 0xFFFFFFFFu;
-  for (int b = 0; b < kFrontBuckets && I.h0 + b <= L; ++b) best = std::min(best, I.goal_key[(size_t)b]);
+  for (size_t b = 0; b < I.goal_key.size() && I.h0 + (int)b <= L; ++b) best = std::min(best, I.goal_key[b]);
   return best == 0xFFFFFFFFu ? -1 : (int)(best & 0xFFFFFFu);
 }
 
 // Smallest maxf of a root-set goal node (INT32_MAX: none).
 int32_t goal_maxf(const Instance &I) {
-  for (int b = 0; b < kFrontBuckets; ++b)
-    if (I.goal_key[(size_t)b] != 0xFFFFFFFFu) return I.h0 + b;
+  for (size_t b = 0; b < I.goal_key.size(); ++b)
+    if (I.goal_key[b] != 0xFFFFFFFFu) return I.h0 + (int)b;
   return 0x7FFFFFFF;
 }
 
