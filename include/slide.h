@@ -163,6 +163,18 @@ int sp_pdb_import(sp_solver *s, int table, const uint8_t *src, uint64_t size);
 /* Heuristic value of n states (tiles n*width*width) into h[n]. */
 int sp_heuristic(sp_solver *s, const uint8_t *tiles, int n, int32_t *h);
 
+/* The root-set template the batch solve uses for a blank at cell `blank`:
+ * the search tree expanded level by level (children in move order, no move
+ * reversing its parent's) until a level holds at least `target` nodes --
+ * the uniform-depth counterpart of create_root_set
+ * (src/24puzzle_block_parallel_with_pdb.cu:454-490).  Writes the number of
+ * nodes, the depth D (the leaves are the level-D nodes) and the number of
+ * leaves, and the first min(cap, nodes) nodes in breadth-first order as
+ * their moves from the root (2 bits per move, first move lowest).  Host
+ * only, needs no GPU. */
+int sp_root_set_template(int width, int blank, int target, uint64_t *paths, uint32_t cap, uint32_t *n_nodes,
+                         uint32_t *depth, uint32_t *n_leaves);
+
 /* Solve n instances, results[n].  Replaces input_table() + ida_star()
  * (src/24puzzle_block_parallel_with_pdb.cu:433-452, :756-922), batched: all
  * instances share each threshold round's kernel launch. */

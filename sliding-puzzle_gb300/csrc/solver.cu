@@ -1683,6 +1683,21 @@ int sp_pdb_import(sp_solver *s, int table, const uint8_t *src, uint64_t size) {
   return SP_OK;
 }
 
+int sp_root_set_template(int width, int blank, int target, uint64_t *paths, uint32_t cap, uint32_t *n_nodes,
+                         uint32_t *depth, uint32_t *n_leaves) {
+  if ((width != 4 && width != 5) || blank < 0 || blank >= width * width || target < 1 || target > (1 << 20) ||
+      (cap && !paths) || !n_nodes || !depth || !n_leaves)
+    return SP_ERR_ARG;
+  FrontTemplate T;
+  if (!build_template(width, blank, target, T)) return SP_ERR_CAPACITY;
+  const uint32_t n = (uint32_t)T.path.size();
+  *n_nodes = n;
+  *depth = T.D;
+  *n_leaves = T.lev[T.D + 1] - T.lev[T.D];
+  for (uint32_t x = 0; x < std::min(cap, n); ++x) paths[x] = T.path[x];
+  return SP_OK;
+}
+
 int sp_heuristic(sp_solver *s, const uint8_t *tiles, int n, int32_t *h) {
   if (!s || (n > 0 && (!tiles || !h)) || n < 0) return SP_ERR_ARG;
   if (s->heur == SP_HEUR_PDB && !s->pdb_ready) return SP_ERR_NO_PDB;

@@ -113,6 +113,7 @@ def load(build=True):
         "sp_probe_random_sectors": (I32, [U64, I32, I32, P, P]),
         "sp_dfs_round_md_noalloc": (I32, [I32, P, P, P, I32, I32, P, P, P]),
         "sp_idas_parallel": (I32, [P, I32, P, I32, P, P, P]),
+        "sp_root_set_template": (I32, [I32, I32, I32, P, ctypes.c_uint32, P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -120,6 +121,20 @@ def load(build=True):
         fn.argtypes = args
     _lib = lib
     return lib
+
+
+def root_set_template(width, blank, target, cap=0):
+    """The root-set template of a blank cell (host only, no GPU): (nodes,
+    depth, leaves, paths) with paths the first `cap` nodes in breadth-first
+    order as 2-bit move sequences from the root, first move lowest."""
+    lib = load()
+    paths = np.zeros(max(cap, 1), dtype=np.uint64)
+    n, d, nl = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+    st = lib.sp_root_set_template(int(width), int(blank), int(target), paths.ctypes.data, int(cap),
+                                  ctypes.byref(n), ctypes.byref(d), ctypes.byref(nl))
+    if st != 0:
+        raise SlideError(st, "sp_root_set_template: %s" % lib.sp_status_string(st).decode())
+    return n.value, d.value, nl.value, paths[: min(cap, n.value)]
 
 
 def default_config(**overrides):
