@@ -152,14 +152,6 @@ __device__ __forceinline__ uint32_t set_byte(uint32_t v, int p, uint32_t x) {
 #define SP_MULTI_PIECE 1.0
 #endif
 
-// Multi-iteration mode: the warp of the lane that finished an instance's last
-// task of an iteration completes that iteration (adds the root-set interior
-// count, checks for a goal) and publishes the next iteration's roots -- the
-// threshold loop of src/24puzzle_block_parallel_with_pdb.cu:772-921 run on the
-// device, per instance, with no barrier across instances.  Called by all 32
-// lanes of a warp with the same instance i; `hist` is the warp's 32 words of
-// shared memory.  Kept out of line: it is cold, and inlined its registers
-// would crowd the search loop.
 // Iteration r of instance i, published beside the one before it (warp
 // advance below): its limit and solution record (those of r - 2, whose goal
 // flag is clear), loads zeroed, its na roots (in maxf order, unsplit) at
@@ -199,6 +191,16 @@ __device__ __noinline__ void publish_second(const RoundParams &P, uint32_t i, in
   __syncwarp();
 }
 
+// Multi-iteration mode: the warp of the lane that finished an instance's last
+// task of an iteration completes that iteration (adds the root-set interior
+// count, checks for a goal) and publishes the next iteration's roots -- the
+// threshold loop of src/24puzzle_block_parallel_with_pdb.cu:772-921 run on the
+// device, per instance, with no barrier across instances.  Called by all 32
+// lanes of a warp with the same instance i; `hist` is the warp's 32 words of
+// shared memory.  Kept out of line: it is cold, and inlined its registers
+// would crowd the search loop.  When the instance's next iteration is
+// predicted small (below P.pair_nodes) it is published together with this
+// one, and the call that completes such a pair settles both in order.
 __device__ __noinline__ void warp_advance(const RoundParams &P, uint32_t i, uint32_t *hist) {
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
