@@ -75,3 +75,11 @@ def test_template_argument_checks():
         st = lib.sp_root_set_template(args[0], args[1], args[2], None, 0, ctypes.byref(n), ctypes.byref(d),
                                       ctypes.byref(nl))
         assert st == -1, args
+
+
+def test_template_at_the_largest_target():
+    # the largest configurable root set (2^20 per instance) stays within the
+    # 64-bit move encoding and the 24-bit node numbering of the goal records
+    for width, blank in ((4, 0), (5, 12)):
+        n, d, nl, _ = slide.root_set_template(width, blank, 1 << 20)
+        assert nl >= 1 << 20 and d <= 32 and n < 1 << 24
